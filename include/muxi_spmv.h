@@ -1,0 +1,324 @@
+/*
+ * muxi_spmv.h -- C ABI of the GB300 (sm_103a) SpMV library.
+ *
+ * This is the drop-in boundary for the muxi_spmv "handle / matrix / format
+ * conversion / execute" path.  Every entry point takes plain pointers and
+ * sizes (device pointers unless the name says "host"), returns a
+ * spmv_status_t and never throws.  The reference exposes the same operations
+ * as C++ templates in namespace muxi_spmv; include/muxi_spmv.hpp maps those
+ * template names onto the _f32 / _f64 entry points declared here.
+ *
+ * Reference interfaces replaced (paths inside the muxi_spmv project):
+ *   src/utils/common.h:31-94          status / format / type / op enums, opts
+ *   src/api/spmv_api.h:18-92          handle, spmv_exec, spmv_csr_exec
+ *   src/spmv/csr/spmv_csr.cu:52-249   spmv_csr<T> dispatcher
+ *   src/spmv/csr5/spmv_csr5.cu:223-362  csr5_preprocess<T>, spmv_csr5<T>
+ *   src/spmv/csr5/spmv_csr5.cu:497-533,912-1014  merge-path search,
+ *                                      partitions, spmv_merge_based<T>
+ *   src/spmv/ellpack/spmv_ellpack.cu:11-91  csr_to_ellpack<T>, spmv_ellpack<T>
+ *   src/preprocessing/column_reorder.cuh:42-201  column reorders
+ *   tests/test_row_reordering.cu:99-143, tests/test_combined_optimizations.cu:176-181
+ *   tests/test_column_reordering.cu:116-199  row / "RCM" / frequency reorders
+ *   src/generators/matrix_generator.h:19-102  synthetic matrix generators
+ *
+ * Threading: a handle is not thread safe (same as the reference).  All device
+ * work is asynchronous on the stream given (opts->stream or the handle's
+ * stream) unless opts->sync is set.
+ */
+#ifndef MUXI_SPMV_H_
+#define MUXI_SPMV_H_
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MUXI_SPMV_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define SPMV_API __attribute__((visibility("default")))
+#else
+#define SPMV_API
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Enums and options: same names and numeric values as                 */
+/* src/utils/common.h:31-94.                                            */
+/* ------------------------------------------------------------------ */
+typedef enum {
+    SPMV_SUCCESS = 0,
+    SPMV_ERROR_INVALID_HANDLE = -1,
+    SPMV_ERROR_INVALID_MATRIX = -2,
+    SPMV_ERROR_INVALID_VECTOR = -3,
+    SPMV_ERROR_MEMORY_ALLOC = -4,
+    SPMV_ERROR_MEMORY_COPY = -5,
+    SPMV_ERROR_DEVICE = -6,
+    SPMV_ERROR_UNSUPPORTED_FORMAT = -7,
+    SPMV_ERROR_UNSUPPORTED_TYPE = -8,
+    SPMV_ERROR_INTERNAL = -9
+} spmv_status_t;
+
+/* common.h:45-53; ELL has no value in the reference and takes 5 here. */
+typedef enum {
+    SPMV_FORMAT_CSR = 0,
+    SPMV_FORMAT_COO = 1,
+    SPMV_FORMAT_CSR2 = 2,
+    SPMV_FORMAT_BSR = 3,
+    SPMV_FORMAT_CSR5 = 4,
+    SPMV_FORMAT_ELL = 5,
+    SPMV_FORMAT_UNKNOWN = -1
+} spmv_format_t;
+
+/* common.h:55-63 */
+typedef enum {
+    SPMV_TYPE_FLOAT = 0,
+    SPMV_TYPE_DOUBLE = 1,
+    SPMV_TYPE_HALF = 2,
+    SPMV_TYPE_BF16 = 3,
+    SPMV_TYPE_TF32 = 4,
+    SPMV_TYPE_UNKNOWN = -1
+} spmv_type_t;
+
+/* common.h:65-70 */
+typedef enum {
+    SPMV_OP_NORMAL = 0,
+    SPMV_OP_TRANSPOSE = 1,
+    SPMV_OP_CONJUGATE = 2
+} spmv_operation_t;
+
+/* common.h:73-94, field for field.  `stream` holds a cudaStream_t value
+ * (NULL = legacy default stream).  The reference's spmv_set_stream stored a
+ * pointer to the handle's stream member here (spmv_api.cu:53-54); this
+ * library stores the stream itself. */
+typedef struct {
+    spmv_operation_t operation;
+    int sync;
+    int check_inputs;
+    int use_tensor_core;
+    int use_streaming;
+    int stream_id;
+    void* stream;
+} spmv_opts_t;
+
+/* common.h:84-94 */
+SPMV_API spmv_opts_t spmv_default_opts(void);
+
+/* ------------------------------------------------------------------ */
+/* Handle: src/api/spmv_api.h:18-43.  The leading fields are the        */
+/* reference's, in its order; the rest are GB300 additions.            */
+/* ------------------------------------------------------------------ */
+typedef struct spmv_handle_t {
+    int deviceId;
+    cudaStream_t stream;
+    spmv_opts_t opts;
+    int warpSize;
+    int smCount;
+    int maxThreadsPerBlock;
+    size_t sharedMemPerSM;
+    /* additions */
+    size_t l2CacheBytes;
+    size_t sharedMemPerBlockOptin;
+    int ccMajor;
+    int ccMinor;
+    void* internal;
+} spmv_handle_t;
+
+/* spmv_api.cu:11-37 */
+SPMV_API spmv_status_t spmv_create_handle(spmv_handle_t** handle);
+/* spmv_api.cu:39-46 */
+SPMV_API spmv_status_t spmv_destroy_handle(spmv_handle_t* handle);
+/* spmv_api.cu:48-56 (stores the stream by value) */
+SPMV_API spmv_status_t spmv_set_stream(spmv_handle_t* handle, cudaStream_t stream);
+
+/* Text of the last error raised on the calling host thread ("" if none). */
+SPMV_API const char* spmv_last_error(void);
+/* Library ABI version (MUXI_SPMV_ABI_VERSION). */
+SPMV_API int spmv_abi_version(void);
+
+/* ------------------------------------------------------------------ */
+/* CSR SpMV, y = alpha*A*x + beta*y.                                    */
+/* Replaces spmv_csr<T> (src/spmv/csr/spmv_csr.cu:52-249,              */
+/* declared spmv_csr.cuh:1100-1106) and spmv_csr_exec<T>                */
+/* (src/api/spmv_api.h:82-92).  Unlike the reference, alpha and beta    */
+/* are applied; beta == 0 never reads y.  nnz == 0 still writes         */
+/* y = beta*y.  The call is stateless: it runs the load-balanced         */
+/* merge-path kernel and takes its scratch from the stream-ordered      */
+/* allocator of the call's stream.                                      */
+/* ------------------------------------------------------------------ */
+SPMV_API spmv_status_t spmv_csr_f32(int numRows, int numCols, int nnz,
+                           const int* rowPtr, const int* colIdx, const float* values,
+                           const float* x, float* y, float alpha, float beta,
+                           const spmv_opts_t* opts);
+SPMV_API spmv_status_t spmv_csr_f64(int numRows, int numCols, int nnz,
+                           const int* rowPtr, const int* colIdx, const double* values,
+                           const double* x, double* y, double alpha, double beta,
+                           const spmv_opts_t* opts);
+
+/* Kernel variants of the CSR family (the autotuner's search space).
+ * Replaces the reference's fixed choice between spmv_csr_scalar_kernel,
+ * spmv_csr_vector_kernel and the N-threads-per-row family
+ * (spmv_csr.cuh:83-208, tests/test_block_optimization.cu:97-145). */
+typedef enum {
+    SPMV_KERNEL_AUTO = 0,      /* plan: selector decides                    */
+    SPMV_KERNEL_SCALAR = 1,    /* one thread per row                        */
+    SPMV_KERNEL_VECTOR = 2,    /* threadsPerRow lanes per row, 2..32       */
+    SPMV_KERNEL_MERGE = 3,     /* merge-path CTA tiles + carry fix-up       */
+    SPMV_KERNEL_CSR5 = 4,      /* sigma-nnz tiles (CSR5 metadata)           */
+    SPMV_KERNEL_ELL = 5,       /* column-major ELLPACK                      */
+    SPMV_KERNEL_HEURISTIC = 6  /* plan: the reference's avgNnz rule, restated */
+} spmv_kernel_t;
+
+/* One launch configuration of a kernel family. */
+typedef struct {
+    spmv_kernel_t kernel;
+    int blockSize;       /* threads per CTA: 128, 256 or 512               */
+    int threadsPerRow;   /* VECTOR: 1,2,4,8,16,32                          */
+    int itemsPerThread;  /* MERGE: merge items per thread (tile = block*ipt) */
+    int vectorWidth;     /* VECTOR/ELL: 1 or 4 elements per load           */
+} spmv_variant_t;
+
+/* Run one explicit variant (no plan, no selector).  MERGE variants take
+ * their scratch like spmv_csr_*; CSR5/ELL are not accepted here. */
+SPMV_API spmv_status_t spmv_csr_variant_f32(const spmv_variant_t* variant,
+                                   int numRows, int numCols, int nnz,
+                                   const int* rowPtr, const int* colIdx, const float* values,
+                                   const float* x, float* y, float alpha, float beta,
+                                   const spmv_opts_t* opts);
+SPMV_API spmv_status_t spmv_csr_variant_f64(const spmv_variant_t* variant,
+                                   int numRows, int numCols, int nnz,
+                                   const int* rowPtr, const int* colIdx, const double* values,
+                                   const double* x, double* y, double alpha, double beta,
+                                   const spmv_opts_t* opts);
+
+/* ------------------------------------------------------------------ */
+/* Merge path (src/spmv/csr5/spmv_csr5.cu:497-533, 912-1014).           */
+/* ------------------------------------------------------------------ */
+/* Partition count the reference picks for warp 32 (spmv_csr5.cu:941-972):
+ * max(1, min((numRows+nnz)/32, 128*8*8)). */
+SPMV_API int spmv_merge_default_partitions(int numRows, int nnz);
+
+/* compute_merge_partitions_kernel (spmv_csr5.cu:912-925):
+ * pos[t] = min(t*ceil(L/P), L), t = 0..P, L = numRows+nnz.  pos has P+1
+ * entries.  Bit-exact with the reference (int64 arithmetic inside, so L up
+ * to 2^31-1 never overflows). */
+SPMV_API spmv_status_t spmv_merge_partitions(int numRows, int nnz, int numPartitions,
+                                    int* pos, cudaStream_t stream);
+
+/* merge_path_search (spmv_csr5.cu:497-533) for each of `count` diagonals:
+ * (rowIdx[i], nnzIdx[i]) with rowIdx+nnzIdx = diag[i] and
+ * rowPtr[rowIdx] <= nnzIdx <= rowPtr[rowIdx+1].  Bit-exact. */
+SPMV_API spmv_status_t spmv_merge_path_search(const int* rowPtr, int numRows, int nnz,
+                                     const int* diag, int count,
+                                     int* rowIdx, int* nnzIdx, cudaStream_t stream);
+
+/* spmv_merge_based<T> (spmv_csr5.cu:930-1014), with a correct consumer
+ * (the reference double-counts rows split by a partition) and no
+ * per-call cudaMalloc.  y = A*x. */
+SPMV_API spmv_status_t spmv_merge_based_f32(int numRows, int numCols, int nnz,
+                                   const int* rowPtr, const int* colIdx, const float* values,
+                                   const float* x, float* y, cudaStream_t stream);
+SPMV_API spmv_status_t spmv_merge_based_f64(int numRows, int numCols, int nnz,
+                                   const int* rowPtr, const int* colIdx, const double* values,
+                                   const double* x, double* y, cudaStream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Plans: a matrix plus everything one kernel needs precomputed         */
+/* (tile coordinates, scratch, format copies).  This is the GB300       */
+/* native replacement for spmv_exec<T>(handle, format, matrix, ...)     */
+/* (src/api/spmv_api.h:57-65, declared but never defined there).        */
+/* The plan borrows the CSR arrays; they must outlive it.               */
+/* ------------------------------------------------------------------ */
+typedef struct spmv_plan_s* spmv_plan_t;
+
+SPMV_API spmv_status_t spmv_plan_create(spmv_handle_t* handle, spmv_type_t type,
+                               int numRows, int numCols, int nnz,
+                               const int* rowPtr, const int* colIdx, const void* values,
+                               const spmv_variant_t* variant, spmv_plan_t* plan);
+SPMV_API spmv_status_t spmv_plan_destroy(spmv_plan_t plan);
+/* The variant the plan runs (after AUTO / HEURISTIC resolution). */
+SPMV_API spmv_status_t spmv_plan_get_variant(spmv_plan_t plan, spmv_variant_t* variant);
+/* Device bytes the plan holds beyond the borrowed CSR arrays. */
+SPMV_API spmv_status_t spmv_plan_get_workspace_bytes(spmv_plan_t plan, size_t* bytes);
+SPMV_API spmv_status_t spmv_plan_exec_f32(spmv_handle_t* handle, spmv_plan_t plan, float alpha,
+                                 const float* x, float beta, float* y);
+SPMV_API spmv_status_t spmv_plan_exec_f64(spmv_handle_t* handle, spmv_plan_t plan, double alpha,
+                                 const double* x, double beta, double* y);
+
+/* Kernel timing on the launching stream (the role of the reference's
+ * GpuTimer, src/utils/timer.h:17-47, moved into the plan): while enabled,
+ * each exec records a CUDA event pair around the plan's main kernel only
+ * (not the carry fix-up).  spmv_plan_profile_read waits for the recorded
+ * events and returns the summed main-kernel time and the launch count, then
+ * starts a new window.  Enabling resets the window. */
+SPMV_API spmv_status_t spmv_plan_profile(spmv_plan_t plan, int enable);
+SPMV_API spmv_status_t spmv_plan_profile_read(spmv_plan_t plan, double* kernel_ms, int* launches);
+
+/* ------------------------------------------------------------------ */
+/* Matrix statistics.                                                   */
+/* ------------------------------------------------------------------ */
+/* Number of distinct column indices present in colIdx (device bitmap).
+ * Used for the algorithmic-byte count of the x gather. */
+SPMV_API spmv_status_t spmv_count_distinct_columns(int numCols, int nnz, const int* colIdx,
+                                          long long* distinct, cudaStream_t stream);
+/* Validates a device CSR: rowPtr[0]==0, rowPtr monotone, rowPtr[R]==nnz,
+ * 0<=col<numCols.  *bad = number of violations found (0 = valid). */
+SPMV_API spmv_status_t spmv_validate_csr(int numRows, int numCols, int nnz, const int* rowPtr,
+                                const int* colIdx, long long* bad, cudaStream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Seeded synthetic generators (host, multi-threaded, deterministic for */
+/* a given seed whatever the thread count).  Replaces the libc-rand()   */
+/* generators of src/generators/matrix_generator.h:19-102.              */
+/* Two steps: spmv_gen_row_ptr fills rowPtr (numRows+1, host) and       */
+/* returns nnz; spmv_gen_fill_* then fills colIdx/values (host).        */
+/* ------------------------------------------------------------------ */
+typedef enum {
+    SPMV_GEN_POISSON_UNIFORM = 0,  /* Poisson(p0) lengths clamped to [p1,p2];
+                                      columns uniform without replacement,
+                                      sorted; values U[-1,1]                  */
+    SPMV_GEN_POWERLAW = 1,         /* Zipf(p0) lengths truncated to [1,p1];
+                                      fraction p3 of columns within +-p2 of
+                                      the diagonal, rest uniform; sorted;
+                                      values N(0,1)                           */
+    SPMV_GEN_STENCIL2D = 2,        /* 5-point on a p0 x p1 grid; 4 / -1       */
+    SPMV_GEN_STENCIL3D = 3,        /* 27-point on a p0 x p1 x p2 grid; N(0,1) */
+    SPMV_GEN_BANDED = 4,           /* lengths Poisson(p0) clamped [1,p1],
+                                      columns within the band of width p1    */
+    SPMV_GEN_BLOCKDIAG = 5,        /* p0 diagonal blocks; Poisson(p1) lengths
+                                      clamped to the block; columns uniform
+                                      inside the block                        */
+    SPMV_GEN_ZIPF_UNIFORM = 6,     /* Zipf(p0) lengths truncated to [1,p1],
+                                      columns uniform without replacement     */
+    SPMV_GEN_DIAGONAL = 7          /* identity pattern, values 1              */
+} spmv_gen_kind_t;
+
+typedef struct {
+    spmv_gen_kind_t kind;
+    int numRows;
+    int numCols;
+    double p0, p1, p2, p3;
+    unsigned long long seed;
+    int threads;                   /* 0 = all hardware threads */
+} spmv_gen_params_t;
+
+/* Fills rowPtr[0..numRows] and returns nnz in *nnz (int64; the call fails
+ * with SPMV_ERROR_INVALID_MATRIX if nnz >= 2^31). */
+SPMV_API spmv_status_t spmv_gen_row_ptr(const spmv_gen_params_t* p, int* rowPtr, long long* nnz);
+SPMV_API spmv_status_t spmv_gen_fill_f32(const spmv_gen_params_t* p, const int* rowPtr,
+                                int* colIdx, float* values);
+SPMV_API spmv_status_t spmv_gen_fill_f64(const spmv_gen_params_t* p, const int* rowPtr,
+                                int* colIdx, double* values);
+/* Dense vector with entries U[lo,hi] (host). */
+SPMV_API spmv_status_t spmv_gen_vector_f32(long long n, unsigned long long seed, double lo, double hi,
+                                  float* out, int threads);
+SPMV_API spmv_status_t spmv_gen_vector_f64(long long n, unsigned long long seed, double lo, double hi,
+                                  double* out, int threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MUXI_SPMV_H_ */

@@ -1,0 +1,135 @@
+"""ctypes binding of libmuxispmv.so (the C ABI declared in include/muxi_spmv.h).
+
+The shared library is built in-tree by muxi_spmv_gb300.build.  Loading fails
+loudly when it is missing: there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+# Status codes (src/utils/common.h:31-43).
+SPMV_SUCCESS = 0
+STATUS_NAMES = {
+    0: "SPMV_SUCCESS", -1: "SPMV_ERROR_INVALID_HANDLE", -2: "SPMV_ERROR_INVALID_MATRIX",
+    -3: "SPMV_ERROR_INVALID_VECTOR", -4: "SPMV_ERROR_MEMORY_ALLOC", -5: "SPMV_ERROR_MEMORY_COPY",
+    -6: "SPMV_ERROR_DEVICE", -7: "SPMV_ERROR_UNSUPPORTED_FORMAT", -8: "SPMV_ERROR_UNSUPPORTED_TYPE",
+    -9: "SPMV_ERROR_INTERNAL",
+}
+
+SPMV_TYPE_FLOAT, SPMV_TYPE_DOUBLE = 0, 1
+SPMV_OP_NORMAL, SPMV_OP_TRANSPOSE = 0, 1
+
+KERNEL_AUTO, KERNEL_SCALAR, KERNEL_VECTOR, KERNEL_MERGE, KERNEL_CSR5, KERNEL_ELL, KERNEL_HEURISTIC = range(7)
+
+
+class SpmvError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str):
+        self.status = status
+        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)} ({status}): {detail}")
+
+
+class Opts(C.Structure):
+    """spmv_opts_t (src/utils/common.h:73-82)."""
+    _fields_ = [("operation", C.c_int), ("sync", C.c_int), ("check_inputs", C.c_int),
+                ("use_tensor_core", C.c_int), ("use_streaming", C.c_int), ("stream_id", C.c_int),
+                ("stream", C.c_void_p)]
+
+
+class Handle(C.Structure):
+    """spmv_handle_t (src/api/spmv_api.h:18-28 plus GB300 fields)."""
+    _fields_ = [("deviceId", C.c_int), ("stream", C.c_void_p), ("opts", Opts), ("warpSize", C.c_int),
+                ("smCount", C.c_int), ("maxThreadsPerBlock", C.c_int), ("sharedMemPerSM", C.c_size_t),
+                ("l2CacheBytes", C.c_size_t), ("sharedMemPerBlockOptin", C.c_size_t), ("ccMajor", C.c_int),
+                ("ccMinor", C.c_int), ("internal", C.c_void_p)]
+
+
+class Variant(C.Structure):
+    """spmv_variant_t."""
+    _fields_ = [("kernel", C.c_int), ("blockSize", C.c_int), ("threadsPerRow", C.c_int),
+                ("itemsPerThread", C.c_int), ("vectorWidth", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class GenParams(C.Structure):
+    """spmv_gen_params_t."""
+    _fields_ = [("kind", C.c_int), ("numRows", C.c_int), ("numCols", C.c_int), ("p0", C.c_double),
+                ("p1", C.c_double), ("p2", C.c_double), ("p3", C.c_double), ("seed", C.c_ulonglong),
+                ("threads", C.c_int)]
+
+
+P = C.c_void_p
+I = C.c_int
+F = C.c_float
+D = C.c_double
+S = C.c_int  # spmv_status_t
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "spmv_default_opts": (Opts, []),
+    "spmv_create_handle": (S, [C.POINTER(C.POINTER(Handle))]),
+    "spmv_destroy_handle": (S, [C.POINTER(Handle)]),
+    "spmv_set_stream": (S, [C.POINTER(Handle), P]),
+    "spmv_last_error": (C.c_char_p, []),
+    "spmv_abi_version": (I, []),
+    "spmv_csr_f32": (S, [I, I, I, P, P, P, P, P, F, F, C.POINTER(Opts)]),
+    "spmv_csr_f64": (S, [I, I, I, P, P, P, P, P, D, D, C.POINTER(Opts)]),
+    "spmv_csr_variant_f32": (S, [C.POINTER(Variant), I, I, I, P, P, P, P, P, F, F, C.POINTER(Opts)]),
+    "spmv_csr_variant_f64": (S, [C.POINTER(Variant), I, I, I, P, P, P, P, P, D, D, C.POINTER(Opts)]),
+    "spmv_merge_default_partitions": (I, [I, I]),
+    "spmv_merge_partitions": (S, [I, I, I, P, P]),
+    "spmv_merge_path_search": (S, [P, I, I, P, I, P, P, P]),
+    "spmv_merge_based_f32": (S, [I, I, I, P, P, P, P, P, P]),
+    "spmv_merge_based_f64": (S, [I, I, I, P, P, P, P, P, P]),
+    "spmv_plan_create": (S, [C.POINTER(Handle), I, I, I, I, P, P, P, C.POINTER(Variant), C.POINTER(P)]),
+    "spmv_plan_destroy": (S, [P]),
+    "spmv_plan_get_variant": (S, [P, C.POINTER(Variant)]),
+    "spmv_plan_get_workspace_bytes": (S, [P, C.POINTER(C.c_size_t)]),
+    "spmv_plan_exec_f32": (S, [C.POINTER(Handle), P, F, P, F, P]),
+    "spmv_plan_exec_f64": (S, [C.POINTER(Handle), P, D, P, D, P]),
+    "spmv_plan_profile": (S, [P, I]),
+    "spmv_plan_profile_read": (S, [P, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "spmv_count_distinct_columns": (S, [I, I, P, C.POINTER(C.c_longlong), P]),
+    "spmv_validate_csr": (S, [I, I, I, P, P, C.POINTER(C.c_longlong), P]),
+    "spmv_gen_row_ptr": (S, [C.POINTER(GenParams), P, C.POINTER(C.c_longlong)]),
+    "spmv_gen_fill_f32": (S, [C.POINTER(GenParams), P, P, P]),
+    "spmv_gen_fill_f64": (S, [C.POINTER(GenParams), P, P, P]),
+    "spmv_gen_vector_f32": (S, [C.c_longlong, C.c_ulonglong, D, D, P, I]),
+    "spmv_gen_vector_f64": (S, [C.c_longlong, C.c_ulonglong, D, D, P, I]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads (building if needed) libmuxispmv.so and declares every entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        if os.environ.get("MUXI_SPMV_NO_BUILD"):
+            raise ImportError(f"{LIB_PATH} is missing; run __graft_entry__.build() first")
+        _build.build()
+    L = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return (lib().spmv_last_error() or b"").decode(errors="replace")
+
+
+def check(status: int, where: str) -> None:
+    if status != SPMV_SUCCESS:
+        raise SpmvError(status, where, last_error())

@@ -1,0 +1,317 @@
+"""Python mirror of the muxi_spmv interface over the C ABI.
+
+Names, argument order and meaning follow the reference's C++ API
+(src/api/spmv_api.h, src/spmv/csr/spmv_csr.cuh, src/spmv/csr5/spmv_csr5.cuh,
+src/formats/sparse_formats.h) so tests read like the reference's own.  Device
+memory is held in torch tensors (plumbing only); every computation runs in
+libmuxispmv.so.  Errors raise SpmvError carrying the spmv_status_t.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import (GenParams, Opts, SpmvError, Variant, check, lib, KERNEL_AUTO, KERNEL_SCALAR,  # noqa: F401
+                   KERNEL_VECTOR, KERNEL_MERGE, KERNEL_CSR5, KERNEL_ELL, KERNEL_HEURISTIC,
+                   SPMV_TYPE_FLOAT, SPMV_TYPE_DOUBLE)
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _ptr(t) -> int | None:
+    if t is None:
+        return None
+    return t.data_ptr()
+
+
+def _stream_ptr(stream) -> int | None:
+    """Accepts None (current torch stream), a torch.cuda.Stream or a raw handle."""
+    if stream is None:
+        torch = _torch()
+        return torch.cuda.current_stream().cuda_stream or None
+    if isinstance(stream, int):
+        return stream or None
+    return stream.cuda_stream or None
+
+
+def spmv_default_opts(stream=None, sync: bool = False) -> Opts:
+    o = lib().spmv_default_opts()
+    o.stream = _stream_ptr(stream)
+    o.sync = 1 if sync else 0
+    return o
+
+
+# ---------------------------------------------------------------------------
+# Matrices
+# ---------------------------------------------------------------------------
+class CSRMatrix:
+    """CSRMatrix<T> (src/formats/sparse_formats.h:24-103): host arrays
+    (rowPtr, colIdx, values as numpy) and device arrays (d_* as torch
+    tensors).  The device arrays are owned by torch."""
+
+    def __init__(self, rowPtr, colIdx, values, numCols: int):
+        self.rowPtr = np.ascontiguousarray(rowPtr, np.int32)
+        self.colIdx = np.ascontiguousarray(colIdx, np.int32)
+        self.values = np.ascontiguousarray(values)
+        if self.values.dtype not in (np.float32, np.float64):
+            raise TypeError("values must be float32 or float64")
+        self.numRows = len(self.rowPtr) - 1
+        self.numCols = int(numCols)
+        self.nnz = int(self.rowPtr[-1]) if self.numRows >= 0 and len(self.rowPtr) else 0
+        self.d_rowPtr = self.d_colIdx = self.d_values = None
+
+    @property
+    def dtype(self):
+        return self.values.dtype
+
+    def allocateDevice(self, device="cuda"):
+        torch = _torch()
+        tdt = torch.float32 if self.dtype == np.float32 else torch.float64
+        self.d_rowPtr = torch.empty(self.numRows + 1, dtype=torch.int32, device=device)
+        self.d_colIdx = torch.empty(max(self.nnz, 1), dtype=torch.int32, device=device)
+        self.d_values = torch.empty(max(self.nnz, 1), dtype=tdt, device=device)
+        return self
+
+    def copyToDevice(self, device="cuda"):
+        torch = _torch()
+        if self.d_rowPtr is None:
+            self.allocateDevice(device)
+        self.d_rowPtr.copy_(torch.from_numpy(self.rowPtr))
+        if self.nnz:
+            self.d_colIdx[: self.nnz].copy_(torch.from_numpy(self.colIdx))
+            self.d_values[: self.nnz].copy_(torch.from_numpy(self.values))
+        return self
+
+    def device_args(self):
+        return (self.numRows, self.numCols, self.nnz, _ptr(self.d_rowPtr), _ptr(self.d_colIdx),
+                _ptr(self.d_values))
+
+
+# ---------------------------------------------------------------------------
+# Handle (src/api/spmv_api.h:18-43)
+# ---------------------------------------------------------------------------
+class SpmvHandle:
+    def __init__(self):
+        h = C.POINTER(_lib.Handle)()
+        check(lib().spmv_create_handle(C.byref(h)), "spmv_create_handle")
+        self._h = h
+
+    @property
+    def raw(self):
+        return self._h
+
+    def __getattr__(self, name):
+        if name.startswith("_"):
+            raise AttributeError(name)
+        return getattr(self._h.contents, name)
+
+    def set_stream(self, stream):
+        check(lib().spmv_set_stream(self._h, _stream_ptr(stream)), "spmv_set_stream")
+
+    def destroy(self):
+        if self._h:
+            check(lib().spmv_destroy_handle(self._h), "spmv_destroy_handle")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def spmv_create_handle() -> SpmvHandle:
+    return SpmvHandle()
+
+
+def spmv_destroy_handle(h: SpmvHandle):
+    h.destroy()
+
+
+def spmv_set_stream(h: SpmvHandle, stream):
+    h.set_stream(stream)
+
+
+# ---------------------------------------------------------------------------
+# Execution
+# ---------------------------------------------------------------------------
+def _is_f32(A: CSRMatrix) -> bool:
+    return A.dtype == np.float32
+
+
+def spmv_csr(A: CSRMatrix, x, y, alpha=1.0, beta=0.0, opts: Opts | None = None):
+    """spmv_csr<T> (src/spmv/csr/spmv_csr.cu:52-249) with alpha/beta applied."""
+    o = opts if opts is not None else spmv_default_opts()
+    f = lib().spmv_csr_f32 if _is_f32(A) else lib().spmv_csr_f64
+    check(f(*A.device_args(), _ptr(x), _ptr(y), alpha, beta, C.byref(o)), "spmv_csr")
+    return y
+
+
+def make_variant(kernel: int, blockSize: int = 256, threadsPerRow: int = 0, itemsPerThread: int = 0,
+                 vectorWidth: int = 1) -> Variant:
+    return Variant(kernel, blockSize, threadsPerRow, itemsPerThread, vectorWidth)
+
+
+def spmv_csr_variant(variant: Variant, A: CSRMatrix, x, y, alpha=1.0, beta=0.0, opts: Opts | None = None):
+    o = opts if opts is not None else spmv_default_opts()
+    f = lib().spmv_csr_variant_f32 if _is_f32(A) else lib().spmv_csr_variant_f64
+    check(f(C.byref(variant), *A.device_args(), _ptr(x), _ptr(y), alpha, beta, C.byref(o)), "spmv_csr_variant")
+    return y
+
+
+def spmv_merge_based(A: CSRMatrix, x, y, stream=None):
+    """spmv_merge_based<T> (src/spmv/csr5/spmv_csr5.cu:930-1014): y = A*x."""
+    f = lib().spmv_merge_based_f32 if _is_f32(A) else lib().spmv_merge_based_f64
+    check(f(*A.device_args(), _ptr(x), _ptr(y), _stream_ptr(stream)), "spmv_merge_based")
+    return y
+
+
+def merge_default_partitions(numRows: int, nnz: int) -> int:
+    return lib().spmv_merge_default_partitions(numRows, nnz)
+
+
+def compute_merge_partitions(numRows: int, nnz: int, numPartitions: int, stream=None):
+    """compute_merge_partitions_kernel (spmv_csr5.cu:912-925) -> int32 tensor of P+1 positions."""
+    torch = _torch()
+    pos = torch.empty(numPartitions + 1, dtype=torch.int32, device="cuda")
+    check(lib().spmv_merge_partitions(numRows, nnz, numPartitions, _ptr(pos), _stream_ptr(stream)),
+          "spmv_merge_partitions")
+    return pos
+
+
+def merge_path_search(A: CSRMatrix, diag, stream=None):
+    """merge_path_search (spmv_csr5.cu:497-533) for each diagonal in `diag` (int32 tensor)."""
+    torch = _torch()
+    n = diag.numel()
+    r = torch.empty(n, dtype=torch.int32, device="cuda")
+    z = torch.empty(n, dtype=torch.int32, device="cuda")
+    check(lib().spmv_merge_path_search(_ptr(A.d_rowPtr), A.numRows, A.nnz, _ptr(diag), n, _ptr(r), _ptr(z),
+                                       _stream_ptr(stream)), "spmv_merge_path_search")
+    return r, z
+
+
+class Plan:
+    """A plan binds a device CSR matrix to one kernel variant and its
+    precomputed metadata (tile coordinates, scratch)."""
+
+    def __init__(self, handle: SpmvHandle, A: CSRMatrix, variant: Variant | None = None):
+        self.handle = handle
+        self.A = A  # keeps the borrowed device arrays alive
+        v = variant if variant is not None else make_variant(KERNEL_AUTO)
+        p = C.c_void_p()
+        check(lib().spmv_plan_create(handle.raw, SPMV_TYPE_FLOAT if _is_f32(A) else SPMV_TYPE_DOUBLE,
+                                     *A.device_args(), C.byref(v), C.byref(p)), "spmv_plan_create")
+        self._p = p
+
+    @property
+    def variant(self) -> Variant:
+        v = Variant()
+        check(lib().spmv_plan_get_variant(self._p, C.byref(v)), "spmv_plan_get_variant")
+        return v
+
+    @property
+    def workspace_bytes(self) -> int:
+        b = C.c_size_t()
+        check(lib().spmv_plan_get_workspace_bytes(self._p, C.byref(b)), "spmv_plan_get_workspace_bytes")
+        return b.value
+
+    def exec(self, x, y, alpha=1.0, beta=0.0):
+        f = lib().spmv_plan_exec_f32 if _is_f32(self.A) else lib().spmv_plan_exec_f64
+        check(f(self.handle.raw, self._p, alpha, _ptr(x), beta, _ptr(y)), "spmv_plan_exec")
+        return y
+
+    def profile(self, enable: bool = True):
+        """Records CUDA events around the main kernel of every exec."""
+        check(lib().spmv_plan_profile(self._p, 1 if enable else 0), "spmv_plan_profile")
+
+    def profile_read(self):
+        """(summed main-kernel milliseconds, launches) since profile() / the last read."""
+        ms, n = C.c_double(), C.c_int()
+        check(lib().spmv_plan_profile_read(self._p, C.byref(ms), C.byref(n)), "spmv_plan_profile_read")
+        return ms.value, n.value
+
+    def destroy(self):
+        if self._p:
+            check(lib().spmv_plan_destroy(self._p), "spmv_plan_destroy")
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def count_distinct_columns(A: CSRMatrix, stream=None) -> int:
+    d = C.c_longlong()
+    check(lib().spmv_count_distinct_columns(A.numCols, A.nnz, _ptr(A.d_colIdx), C.byref(d), _stream_ptr(stream)),
+          "spmv_count_distinct_columns")
+    return d.value
+
+
+def validate_csr(A: CSRMatrix, stream=None) -> int:
+    b = C.c_longlong()
+    check(lib().spmv_validate_csr(A.numRows, A.numCols, A.nnz, _ptr(A.d_rowPtr), _ptr(A.d_colIdx), C.byref(b),
+                                  _stream_ptr(stream)), "spmv_validate_csr")
+    return b.value
+
+
+# ---------------------------------------------------------------------------
+# Generators (host)
+# ---------------------------------------------------------------------------
+GEN_POISSON_UNIFORM, GEN_POWERLAW, GEN_STENCIL2D, GEN_STENCIL3D, GEN_BANDED, GEN_BLOCKDIAG, GEN_ZIPF_UNIFORM, \
+    GEN_DIAGONAL = range(8)
+
+
+@dataclass
+class GenSpec:
+    kind: int
+    numRows: int
+    numCols: int
+    p0: float = 0.0
+    p1: float = 0.0
+    p2: float = 0.0
+    p3: float = 0.0
+    seed: int = 0
+
+    def params(self, threads: int = 0) -> GenParams:
+        return GenParams(self.kind, self.numRows, self.numCols, self.p0, self.p1, self.p2, self.p3, self.seed,
+                         threads)
+
+
+def generate(spec: GenSpec, dtype=np.float32, threads: int = 0, pinned: bool = False):
+    """Returns host (rowPtr, colIdx, values) numpy arrays for `spec`.
+    pinned=True places the arrays in page-locked memory (torch)."""
+    p = spec.params(threads)
+    rowPtr = np.empty(spec.numRows + 1, np.int32)
+    nnz = C.c_longlong()
+    check(lib().spmv_gen_row_ptr(C.byref(p), rowPtr.ctypes.data_as(C.c_void_p), C.byref(nnz)), "spmv_gen_row_ptr")
+    n = nnz.value
+    if pinned:
+        torch = _torch()
+        tdt = torch.float32 if dtype == np.float32 else torch.float64
+        colIdx = torch.empty(max(n, 1), dtype=torch.int32, pin_memory=True).numpy()[:n]
+        values = torch.empty(max(n, 1), dtype=tdt, pin_memory=True).numpy()[:n]
+    else:
+        colIdx = np.empty(n, np.int32)
+        values = np.empty(n, dtype)
+    f = lib().spmv_gen_fill_f32 if dtype == np.float32 else lib().spmv_gen_fill_f64
+    check(f(C.byref(p), rowPtr.ctypes.data_as(C.c_void_p), colIdx.ctypes.data_as(C.c_void_p),
+            values.ctypes.data_as(C.c_void_p)), "spmv_gen_fill")
+    return rowPtr, colIdx, values
+
+
+def gen_vector(n: int, seed: int, lo: float = -1.0, hi: float = 1.0, dtype=np.float32, threads: int = 0, out=None):
+    v = out if out is not None else np.empty(n, dtype)
+    f = lib().spmv_gen_vector_f32 if v.dtype == np.float32 else lib().spmv_gen_vector_f64
+    check(f(n, seed, lo, hi, v.ctypes.data_as(C.c_void_p), threads), "spmv_gen_vector")
+    return v
+
+
+__all__ = [n for n in dir() if not n.startswith("_")]

@@ -1,0 +1,71 @@
+// Host-side internals shared by the translation units of libmuxispmv.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "muxi_spmv.h"
+
+namespace mxs {
+
+// Records a message for spmv_last_error() on the calling host thread.
+void set_error(const char* file, int line, const char* fmt, ...);
+void clear_error();
+
+// Maps a CUDA error to SPMV_ERROR_DEVICE and records its text.
+spmv_status_t cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+inline cudaStream_t opts_stream(const spmv_opts_t* o) {
+    return (o && o->stream) ? reinterpret_cast<cudaStream_t>(o->stream) : (cudaStream_t)0;
+}
+
+// Launch shape helpers.
+inline unsigned grid_for(long long work, int per_block) {
+    long long g = (work + per_block - 1) / per_block;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+// Internal state hanging off spmv_handle_t::internal.
+struct HandleState {
+    int device = 0;
+};
+
+// Per-device properties cached on first use (SM count, L2 size, smem).
+struct DeviceProps {
+    int sm_count = 0;
+    size_t l2_bytes = 0;
+    size_t smem_optin = 0;
+    int cc_major = 0, cc_minor = 0;
+};
+const DeviceProps& device_props(int dev);
+
+// Returns the current device's SM count (cached).
+int current_sm_count();
+
+}  // namespace mxs
+
+#define MXS_CUDA(expr)                                                        \
+    do {                                                                      \
+        cudaError_t e_ = (expr);                                              \
+        if (e_ != cudaSuccess) return mxs::cuda_fail(e_, #expr, __FILE__, __LINE__); \
+    } while (0)
+
+#define MXS_LAUNCH_CHECK()                                                    \
+    do {                                                                      \
+        cudaError_t e_ = cudaGetLastError();                                  \
+        if (e_ != cudaSuccess) return mxs::cuda_fail(e_, "kernel launch", __FILE__, __LINE__); \
+    } while (0)
+
+#define MXS_FAIL(status, ...)                                                 \
+    do {                                                                      \
+        mxs::set_error(__FILE__, __LINE__, __VA_ARGS__);                      \
+        return (status);                                                      \
+    } while (0)
+
+#define MXS_TRY(expr)                                                         \
+    do {                                                                      \
+        spmv_status_t s_ = (expr);                                            \
+        if (s_ != SPMV_SUCCESS) return s_;                                    \
+    } while (0)

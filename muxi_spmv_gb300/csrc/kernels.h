@@ -1,0 +1,77 @@
+// Launch wrappers exported by the kernel translation units to api.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include "muxi_spmv.h"
+
+namespace mxs {
+
+template <typename T>
+struct RowsArgs {
+    int numRows;
+    int nnz;
+    const int* rowPtr;
+    const int* colIdx;
+    const T* values;
+    const T* x;
+    T* y;
+    T alpha;
+    T beta;
+    int betaZero;
+};
+
+// Scalar / vector CSR kernels (csr_kernels.cu).
+template <typename T>
+spmv_status_t run_rows(int block, int tpr, int vec, const RowsArgs<T>& a, cudaStream_t s);
+// y = beta*y.
+template <typename T>
+spmv_status_t run_scale(long long n, T* y, T beta, cudaStream_t s);
+
+// ---- merge path (merge_kernels.cu) ----
+// Merge-path tile geometry for a given block size / items per thread.
+struct MergeGeom {
+    int block;
+    int ipt;
+    long long tile() const { return (long long)block * ipt; }
+};
+bool merge_geom_supported(int block, int ipt);
+// Number of tiles for a matrix: ceil((R+N)/tile), at least 1.
+long long merge_tile_count(int numRows, int nnz, const MergeGeom& g);
+// Bytes of scratch the merge path needs for P tiles and value size vsize:
+// (P+1) start rows, (P+1) start nnz, P carry rows, P carry values.
+size_t merge_scratch_bytes(long long P, size_t vsize);
+
+struct MergeScratch {
+    int* tileRow;   // P+1
+    int* tileNnz;   // P+1
+    int* carryRow;  // P
+    void* carryVal; // P values
+};
+// Carves the four arrays out of one buffer of merge_scratch_bytes().
+MergeScratch merge_carve(void* base, long long P, size_t vsize);
+
+// Tile start coordinates: diagonal min(t*tile, R+N) for t = 0..P.
+spmv_status_t merge_tile_coords(const int* rowPtr, int numRows, int nnz, const MergeGeom& g,
+                                long long P, int* tileRow, int* tileNnz, cudaStream_t s);
+
+// Tile kernel then carry fix-up; `afterMain` (optional) is recorded between them.
+template <typename T>
+spmv_status_t run_merge(const MergeGeom& g, long long P, const MergeScratch& sc, const RowsArgs<T>& a,
+                        cudaStream_t s, cudaEvent_t afterMain = nullptr);
+
+// Reference-compatible partitioning (spmv_csr5.cu:912-925) and search (:497-533).
+spmv_status_t merge_partitions(int numRows, int nnz, int P, int* pos, cudaStream_t s);
+spmv_status_t merge_search(const int* rowPtr, int numRows, int nnz, const int* diag, int count,
+                           int* rowIdx, int* nnzIdx, cudaStream_t s);
+
+// ---- statistics (stats_kernels.cu) ----
+spmv_status_t count_distinct_columns(int numCols, int nnz, const int* colIdx, long long* out,
+                                     cudaStream_t s);
+spmv_status_t validate_csr(int numRows, int numCols, int nnz, const int* rowPtr, const int* colIdx,
+                           long long* bad, cudaStream_t s);
+
+// Stream-ordered scratch from the library's per-device memory pool.
+spmv_status_t scratch_alloc(void** p, size_t bytes, cudaStream_t s);
+spmv_status_t scratch_free(void* p, cudaStream_t s);
+
+}  // namespace mxs

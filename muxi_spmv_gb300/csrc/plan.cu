@@ -1,0 +1,220 @@
+// Plans: precomputed per-matrix state so repeated SpMVs launch only the hot
+// kernels.  This is the definition of the reference's declared-but-undefined
+// spmv_exec<T>(handle, format, matrix, x, y, alpha, beta)
+// (src/api/spmv_api.h:57-65) in a form a C caller can hold on to.
+#include "internal.h"
+#include "kernels.h"
+#include "plan.h"
+
+namespace mxs {
+
+spmv_variant_t heuristic_variant(int numRows, int nnz) {
+    const int avg = nnz / (numRows > 1 ? numRows : 1);
+    spmv_variant_t v{};
+    v.blockSize = 256;
+    v.vectorWidth = 1;
+    if (avg < 32) {
+        v.kernel = SPMV_KERNEL_SCALAR;
+        v.threadsPerRow = 1;
+    } else {
+        v.kernel = SPMV_KERNEL_VECTOR;
+        v.threadsPerRow = 32;
+    }
+    return v;
+}
+
+static spmv_variant_t resolve(const spmv_variant_t* req, int R, int N) {
+    spmv_variant_t v{};
+    if (req) v = *req;
+    if (v.kernel == SPMV_KERNEL_HEURISTIC) return heuristic_variant(R, N);
+    if (v.kernel == SPMV_KERNEL_AUTO) {
+        v = spmv_variant_t{SPMV_KERNEL_MERGE, 256, 0, 7, 1};
+        return v;
+    }
+    if (!v.blockSize) v.blockSize = 256;
+    if (v.kernel == SPMV_KERNEL_SCALAR) v.threadsPerRow = 1;
+    if (v.kernel == SPMV_KERNEL_VECTOR && !v.threadsPerRow) v.threadsPerRow = 32;
+    if (v.kernel == SPMV_KERNEL_MERGE && !v.itemsPerThread) v.itemsPerThread = 7;
+    if (!v.vectorWidth) v.vectorWidth = 1;
+    return v;
+}
+
+template <typename T>
+static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T* x, T beta, T* y) {
+    clear_error();
+    if (!h) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "handle is NULL");
+    if (!p) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "plan is NULL");
+    const spmv_type_t want = sizeof(T) == 4 ? SPMV_TYPE_FLOAT : SPMV_TYPE_DOUBLE;
+    if (p->type != want) MXS_FAIL(SPMV_ERROR_UNSUPPORTED_TYPE, "plan value type does not match the call");
+    if (p->numRows > 0 && !y) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "y is NULL");
+    if (p->nnz > 0 && !x) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "x is NULL");
+    const cudaStream_t s = h->stream;
+    if (p->numRows == 0) return SPMV_SUCCESS;
+    if (p->nnz == 0) return run_scale<T>(p->numRows, y, beta, s);
+    RowsArgs<T> a{p->numRows, p->nnz, p->rowPtr, p->colIdx, static_cast<const T*>(p->values), x, y,
+                  alpha, beta, beta == T(0)};
+    const spmv_variant_t& v = p->variant;
+    cudaEvent_t evStart = nullptr, evEnd = nullptr;
+    if (p->profiling) {
+        if (p->eventsUsed == p->events.size()) {
+            cudaEvent_t e0, e1;
+            MXS_CUDA(cudaEventCreate(&e0));
+            MXS_CUDA(cudaEventCreate(&e1));
+            p->events.emplace_back(e0, e1);
+        }
+        evStart = p->events[p->eventsUsed].first;
+        evEnd = p->events[p->eventsUsed].second;
+        ++p->eventsUsed;
+        MXS_CUDA(cudaEventRecord(evStart, s));
+    }
+    switch (v.kernel) {
+        case SPMV_KERNEL_SCALAR:
+        case SPMV_KERNEL_VECTOR:
+            MXS_TRY(run_rows<T>(v.blockSize, v.threadsPerRow, v.vectorWidth, a, s));
+            if (evEnd) MXS_CUDA(cudaEventRecord(evEnd, s));
+            break;
+        case SPMV_KERNEL_MERGE:
+            MXS_TRY(run_merge<T>(MergeGeom{v.blockSize, v.itemsPerThread}, p->mergeTiles, p->merge, a, s, evEnd));
+            break;
+        default:
+            MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "plan kernel %d not available", (int)v.kernel);
+    }
+    if (h->opts.sync) MXS_CUDA(cudaStreamSynchronize(s));
+    return SPMV_SUCCESS;
+}
+
+}  // namespace mxs
+
+using namespace mxs;
+
+extern "C" {
+
+spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C, int N, const int* rowPtr,
+                               const int* colIdx, const void* values, const spmv_variant_t* variant,
+                               spmv_plan_t* out) {
+    clear_error();
+    if (!h) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "handle is NULL");
+    if (!out) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "plan pointer is NULL");
+    *out = nullptr;
+    if (type != SPMV_TYPE_FLOAT && type != SPMV_TYPE_DOUBLE)
+        MXS_FAIL(SPMV_ERROR_UNSUPPORTED_TYPE, "only SPMV_TYPE_FLOAT and SPMV_TYPE_DOUBLE are supported");
+    if (R < 0 || C < 0 || N < 0) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "negative dimension");
+    if (R > 0 && !rowPtr) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "rowPtr is NULL");
+    if (N > 0 && (!colIdx || !values)) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "colIdx/values is NULL");
+
+    spmv_plan_s* p = new (std::nothrow) spmv_plan_s();
+    if (!p) MXS_FAIL(SPMV_ERROR_MEMORY_ALLOC, "out of host memory");
+    p->type = type;
+    p->numRows = R;
+    p->numCols = C;
+    p->nnz = N;
+    p->rowPtr = rowPtr;
+    p->colIdx = colIdx;
+    p->values = values;
+    p->device = h->deviceId;
+    p->variant = resolve(variant, R, N);
+    const size_t vs = type == SPMV_TYPE_FLOAT ? 4 : 8;
+
+    spmv_status_t st = SPMV_SUCCESS;
+    const spmv_variant_t& v = p->variant;
+    if (v.kernel == SPMV_KERNEL_MERGE) {
+        MergeGeom g{v.blockSize, v.itemsPerThread};
+        if (!merge_geom_supported(g.block, g.ipt)) {
+            set_error(__FILE__, __LINE__, "unsupported merge shape block=%d ipt=%d", g.block, g.ipt);
+            st = SPMV_ERROR_INTERNAL;
+        } else if (R > 0 && N > 0) {
+            p->mergeTiles = merge_tile_count(R, N, g);
+            const size_t bytes = merge_scratch_bytes(p->mergeTiles, vs);
+            cudaError_t e = cudaMalloc(&p->mergeBuf, bytes);
+            if (e != cudaSuccess) {
+                set_error(__FILE__, __LINE__, "plan allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+                st = SPMV_ERROR_MEMORY_ALLOC;
+            } else {
+                p->workspaceBytes = bytes;
+                p->merge = merge_carve(p->mergeBuf, p->mergeTiles, vs);
+                st = merge_tile_coords(rowPtr, R, N, g, p->mergeTiles, p->merge.tileRow, p->merge.tileNnz,
+                                       h->stream);
+                if (st == SPMV_SUCCESS) {
+                    e = cudaStreamSynchronize(h->stream);
+                    if (e != cudaSuccess) st = cuda_fail(e, "plan build", __FILE__, __LINE__);
+                }
+            }
+        }
+    } else if (v.kernel == SPMV_KERNEL_SCALAR || v.kernel == SPMV_KERNEL_VECTOR) {
+        if (v.threadsPerRow < 1 || v.threadsPerRow > 32 || (v.threadsPerRow & (v.threadsPerRow - 1))) {
+            set_error(__FILE__, __LINE__, "threadsPerRow must be a power of two in [1,32]");
+            st = SPMV_ERROR_INTERNAL;
+        }
+    } else {
+        set_error(__FILE__, __LINE__, "kernel %d is not available for plans yet", (int)v.kernel);
+        st = SPMV_ERROR_UNSUPPORTED_FORMAT;
+    }
+    if (st != SPMV_SUCCESS) {
+        if (p->mergeBuf) cudaFree(p->mergeBuf);
+        delete p;
+        return st;
+    }
+    *out = p;
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_plan_profile(spmv_plan_t p, int enable) {
+    clear_error();
+    if (!p) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "plan is NULL");
+    p->profiling = enable != 0;
+    p->eventsUsed = 0;
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_plan_profile_read(spmv_plan_t p, double* kernel_ms, int* launches) {
+    clear_error();
+    if (!p || !kernel_ms || !launches) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "NULL argument");
+    double total = 0.0;
+    for (size_t i = 0; i < p->eventsUsed; ++i) {
+        MXS_CUDA(cudaEventSynchronize(p->events[i].second));
+        float ms = 0.f;
+        MXS_CUDA(cudaEventElapsedTime(&ms, p->events[i].first, p->events[i].second));
+        total += ms;
+    }
+    *kernel_ms = total;
+    *launches = (int)p->eventsUsed;
+    p->eventsUsed = 0;
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_plan_destroy(spmv_plan_t p) {
+    clear_error();
+    if (!p) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "plan is NULL");
+    for (auto& e : p->events) {
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+    }
+    if (p->mergeBuf) cudaFree(p->mergeBuf);
+    delete p;
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_plan_get_variant(spmv_plan_t p, spmv_variant_t* v) {
+    clear_error();
+    if (!p || !v) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "NULL argument");
+    *v = p->variant;
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_plan_get_workspace_bytes(spmv_plan_t p, size_t* bytes) {
+    clear_error();
+    if (!p || !bytes) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "NULL argument");
+    *bytes = p->workspaceBytes;
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_plan_exec_f32(spmv_handle_t* h, spmv_plan_t p, float alpha, const float* x, float beta,
+                                 float* y) {
+    return plan_exec<float>(h, p, alpha, x, beta, y);
+}
+spmv_status_t spmv_plan_exec_f64(spmv_handle_t* h, spmv_plan_t p, double alpha, const double* x, double beta,
+                                 double* y) {
+    return plan_exec<double>(h, p, alpha, x, beta, y);
+}
+
+}  // extern "C"

@@ -1,0 +1,33 @@
+// Plan object: a borrowed CSR matrix plus what one kernel variant needs.
+#pragma once
+
+#include <utility>
+#include <vector>
+
+#include "internal.h"
+#include "kernels.h"
+
+struct spmv_plan_s {
+    spmv_type_t type = SPMV_TYPE_FLOAT;
+    int numRows = 0, numCols = 0, nnz = 0;
+    const int* rowPtr = nullptr;
+    const int* colIdx = nullptr;
+    const void* values = nullptr;
+    spmv_variant_t variant{};
+    int device = 0;
+    // merge path
+    long long mergeTiles = 0;
+    void* mergeBuf = nullptr;  // tile coordinates + carries (cudaMalloc)
+    mxs::MergeScratch merge{};
+    size_t workspaceBytes = 0;
+    // main-kernel timing (spmv_plan_profile)
+    bool profiling = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;
+    size_t eventsUsed = 0;
+};
+
+namespace mxs {
+// The reference's NVIDIA dispatch rule (spmv_csr.cu:115-153): integer
+// avgNnz = nnz / rows; scalar kernel below 32, one warp per row from 32 up.
+spmv_variant_t heuristic_variant(int numRows, int nnz);
+}  // namespace mxs

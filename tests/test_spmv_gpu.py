@@ -1,0 +1,220 @@
+"""GPU parity of the CSR SpMV kernels against the FP64 CPU oracle, through
+the C ABI.  Bound per row: |y - y_ref| <= tol * sum_j |a_ij x_j| with
+tol = 1e-5 (FP32) and 1e-13 (FP64)."""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import device_csr, tol_for
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def build_cases(mx):
+    from muxi_spmv_gb300 import workloads as W
+    cases = {}
+    cases["poisson16k"] = (*mx.generate(W.spec("poisson16k")), 16384)
+    s = W.scaled("powerlaw8m", 60000, seed=2)
+    cases["powerlaw60k"] = (*mx.generate(s), s.numCols)
+    s = W.scaled("stencil2d_4096", 100 * 100, seed=3)
+    cases["stencil2d"] = (*mx.generate(s), s.numCols)
+    s = W.scaled("stencil3d_256", 20 ** 3, seed=4)
+    cases["stencil3d"] = (*mx.generate(s), s.numCols)
+    # One 65,536-nnz row among short ones (the longest row the power-law law allows).
+    rng = np.random.default_rng(5)
+    lens = np.r_[rng.integers(0, 4, 300), 65536, rng.integers(0, 4, 300)].astype(np.int32)
+    rp = np.r_[0, np.cumsum(lens)].astype(np.int32)
+    cols = 70000
+    ci = np.sort(rng.integers(0, cols, rp[-1]).astype(np.int32))
+    v = rng.standard_normal(rp[-1]).astype(np.float32)
+    cases["longrow"] = (rp, ci, v, cols)
+    # Empty rows everywhere, including leading and trailing runs.
+    lens = np.r_[np.zeros(50), rng.integers(0, 3, 2000) * (rng.random(2000) < 0.4), np.zeros(70)].astype(np.int32)
+    rp = np.r_[0, np.cumsum(lens)].astype(np.int32)
+    ci = rng.integers(0, 500, rp[-1]).astype(np.int32)
+    v = rng.standard_normal(rp[-1]).astype(np.float32)
+    cases["empties"] = (rp, ci, v, 500)
+    cases["one_row"] = (np.array([0, 5], np.int32), np.array([0, 1, 1, 7, 9], np.int32),
+                        np.array([1, 2, 3, 4, 5], np.float32), 10)
+    cases["no_nnz"] = (np.zeros(33, np.int32), np.zeros(0, np.int32), np.zeros(0, np.float32), 33)
+    return cases
+
+
+@pytest.fixture(scope="module")
+def cases(mx):
+    return build_cases(mx)
+
+
+VARIANTS = [("merge", 3, 256, 7, 0, 1), ("merge", 3, 256, 3, 0, 1), ("merge", 3, 256, 11, 0, 1),
+            ("merge", 3, 128, 5, 0, 1), ("merge", 3, 128, 9, 0, 1),
+            ("scalar", 1, 256, 0, 1, 1), ("vec2", 2, 256, 0, 2, 1), ("vec4q", 2, 128, 0, 4, 4),
+            ("vec8", 2, 512, 0, 8, 1), ("vec8q", 2, 256, 0, 8, 4), ("vec16q", 2, 256, 0, 16, 4),
+            ("vec32", 2, 256, 0, 32, 1), ("vec32q", 2, 256, 0, 32, 4), ("vec1q", 2, 256, 0, 1, 4)]
+
+
+def run_variant(mx, cuda, A, x, y, var, alpha, beta):
+    name, kernel, block, ipt, tpr, vw = var
+    v = mx.make_variant(kernel, block, tpr, ipt, vw)
+    mx.spmv_csr_variant(v, A, x, y, alpha, beta)
+    cuda.cuda.synchronize()
+
+
+def check(y_dev, y0, A, x_host, alpha, beta):
+    y = y_dev.cpu().numpy()
+    yr, a = oracle.spmv_ref(A.rowPtr, A.colIdx, A.values, x_host)
+    want = alpha * yr + (beta * y0.astype(np.float64) if beta != 0 else 0.0)
+    scale = abs(alpha) * a + (abs(beta) * np.abs(y0.astype(np.float64)) if beta != 0 else 0.0)
+    tol = tol_for(A.dtype)
+    err = np.abs(y.astype(np.float64) - want)
+    # the epilogue adds one rounding of alpha*s + beta*y in the value type
+    eps = np.finfo(A.dtype).eps
+    bound = tol * scale + 2 * eps * np.abs(want)
+    bad = np.flatnonzero(err > bound)
+    assert bad.size == 0, f"{bad.size} rows out of bound, first {bad[:5]}, err {err[bad[:5]]}, bound {bound[bad[:5]]}"
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+@pytest.mark.parametrize("var", VARIANTS, ids=[v[0] + str(v[3] or "") + "b" + str(v[2]) for v in VARIANTS])
+def test_variants_match_oracle(mx, cuda, cases, var, dtype):
+    torch = cuda
+    for name, (rp, ci, v, cols) in cases.items():
+        A = device_csr(mx, rp, ci, v.astype(dtype), cols)
+        xh = mx.gen_vector(cols, 77, dtype=dtype)
+        x = torch.from_numpy(xh).cuda()
+        for alpha, beta in ((1.0, 0.0), (-0.5, 2.0)):
+            y0 = mx.gen_vector(A.numRows, 99, dtype=dtype)
+            y = torch.from_numpy(y0.copy()).cuda()
+            run_variant(mx, torch, A, x, y, var, alpha, beta)
+            check(y, y0, A, xh, alpha, beta)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_stateless_and_merge_based(mx, cuda, cases, dtype):
+    torch = cuda
+    for name, (rp, ci, v, cols) in cases.items():
+        A = device_csr(mx, rp, ci, v.astype(dtype), cols)
+        xh = mx.gen_vector(cols, 7, dtype=dtype)
+        x = torch.from_numpy(xh).cuda()
+        y = torch.full((max(A.numRows, 1),), float("nan"), dtype=x.dtype, device="cuda")[: A.numRows]
+        mx.spmv_csr(A, x, y)  # beta = 0 never reads y: NaN must not leak
+        torch.cuda.synchronize()
+        check(y, np.zeros(A.numRows, dtype), A, xh, 1.0, 0.0)
+        y2 = torch.full_like(y, float("nan"))
+        mx.spmv_merge_based(A, x, y2)
+        torch.cuda.synchronize()
+        check(y2, np.zeros(A.numRows, dtype), A, xh, 1.0, 0.0)
+
+
+def test_merge_is_deterministic(mx, cuda, cases):
+    torch = cuda
+    rp, ci, v, cols = cases["powerlaw60k"]
+    A = device_csr(mx, rp, ci, v, cols)
+    x = torch.from_numpy(mx.gen_vector(cols, 1)).cuda()
+    ys = []
+    for _ in range(3):
+        y = torch.empty(A.numRows, device="cuda")
+        mx.spmv_csr(A, x, y)
+        ys.append(y.cpu().numpy())
+    assert all(np.array_equal(ys[0], t) for t in ys[1:])
+
+
+def test_kat_diagonal(mx, cuda):
+    """tests/correctness/test_spmv.cu:44-115 through the C ABI."""
+    torch = cuda
+    g = np.load(GOLD / "kat_diagonal.npz")
+    A = device_csr(mx, g["rowPtr"], g["colIdx"], g["values"], len(g["x"]))
+    h = mx.spmv_create_handle()
+    assert h.warpSize == 32 and h.smCount > 0
+    x = torch.from_numpy(g["x"]).cuda()
+    y = torch.zeros_like(x)
+    o = mx.spmv_default_opts(sync=True)
+    mx.spmv_csr(A, x, y, 1.0, 0.0, o)
+    assert np.max(np.abs(y.cpu().numpy() - g["y_expected"])) <= 1e-5
+    h.destroy()
+
+
+@pytest.mark.parametrize("name", ["poisson_2k", "powerlaw_3k", "stencil2d_40", "empty_rows"])
+def test_golden_index_outputs(mx, cuda, name):
+    """Merge partitions and path coordinates from the GPU equal the
+    reference's (golden fixtures from the reference's own code)."""
+    torch = cuda
+    g = dict(np.load(GOLD / f"{name}.npz"))
+    A = device_csr(mx, g["rowPtr"], g["colIdx"], g["values"], int(g["numCols"]))
+    P = int(g["merge_P"])
+    assert mx.merge_default_partitions(A.numRows, A.nnz) == P
+    pos = mx.compute_merge_partitions(A.numRows, A.nnz, P)
+    assert np.array_equal(pos.cpu().numpy(), g["merge_pos"])
+    r, z = mx.merge_path_search(A, torch.from_numpy(g["merge_diag"]).cuda())
+    assert np.array_equal(r.cpu().numpy(), g["merge_row"]) and np.array_equal(z.cpu().numpy(), g["merge_nnz"])
+    # SpMV on the fixture matches the FP64 oracle and bounds the reference loop
+    x = torch.from_numpy(g["x"]).cuda()
+    y = torch.empty(A.numRows, device="cuda")
+    mx.spmv_csr(A, x, y)
+    torch.cuda.synchronize()
+    check(y, np.zeros(A.numRows, np.float32), A, g["x"], 1.0, 0.0)
+
+
+def test_merge_search_all_diagonals(mx, cuda, cases):
+    torch = cuda
+    for name in ("empties", "longrow", "one_row", "no_nnz"):
+        rp, ci, v, cols = cases[name]
+        A = device_csr(mx, rp, ci, v, cols)
+        diag = np.arange(A.numRows + A.nnz + 1, dtype=np.int32)
+        r, z = mx.merge_path_search(A, torch.from_numpy(diag).cuda())
+        r2, z2 = oracle.merge_search(rp, A.nnz, diag)
+        assert np.array_equal(r.cpu().numpy(), r2) and np.array_equal(z.cpu().numpy(), z2)
+        for P in (1, 3, mx.merge_default_partitions(A.numRows, A.nnz)):
+            pos = mx.compute_merge_partitions(A.numRows, A.nnz, P)
+            assert np.array_equal(pos.cpu().numpy(), oracle.merge_partitions(A.numRows, A.nnz, P))
+
+
+def test_plans(mx, cuda, handle, cases):
+    torch = cuda
+    rp, ci, v, cols = cases["powerlaw60k"]
+    for dtype in (np.float32, np.float64):
+        A = device_csr(mx, rp, ci, v.astype(dtype), cols)
+        xh = mx.gen_vector(cols, 3, dtype=dtype)
+        x = torch.from_numpy(xh).cuda()
+        for var in (None, mx.make_variant(mx.KERNEL_HEURISTIC), mx.make_variant(mx.KERNEL_MERGE, 128, 0, 9),
+                    mx.make_variant(mx.KERNEL_VECTOR, 256, 8, 0, 4)):
+            p = mx.Plan(handle, A, var)
+            y0 = mx.gen_vector(A.numRows, 4, dtype=dtype)
+            y = torch.from_numpy(y0.copy()).cuda()
+            p.exec(x, y, 1.5, -1.0)
+            torch.cuda.synchronize()
+            check(y, y0, A, xh, 1.5, -1.0)
+            p.destroy()
+    # heuristic resolves to the reference's rule (avgNnz < 32 -> scalar)
+    A = device_csr(mx, rp, ci, v, cols)
+    p = mx.Plan(handle, A, mx.make_variant(mx.KERNEL_HEURISTIC))
+    assert p.variant.kernel == mx.KERNEL_SCALAR
+    p.destroy()
+
+
+def test_stats(mx, cuda, cases):
+    for name in ("powerlaw60k", "empties", "no_nnz"):
+        rp, ci, v, cols = cases[name]
+        A = device_csr(mx, rp, ci, v, cols)
+        assert mx.count_distinct_columns(A) == oracle.distinct_columns(ci, cols)
+        assert mx.validate_csr(A) == 0
+    rp, ci, v, cols = cases["powerlaw60k"]
+    bad = ci.copy()
+    bad[[3, 10, 99]] = cols + 5
+    A = device_csr(mx, rp, bad, v, cols)
+    assert mx.validate_csr(A) == 3
+
+
+def test_errors_on_device(mx, cuda, handle, cases):
+    rp, ci, v, cols = cases["poisson16k"]
+    A = device_csr(mx, rp, ci, v, cols)
+    with pytest.raises(mx.SpmvError) as e:
+        mx.spmv_csr_variant(mx.make_variant(mx.KERNEL_MERGE, 256, 0, 6), A, A.d_values, A.d_values)
+    assert e.value.status == -9
+    with pytest.raises(mx.SpmvError) as e:
+        mx.Plan(handle, A, mx.make_variant(mx.KERNEL_VECTOR, 256, 3))
+    assert e.value.status == -9
