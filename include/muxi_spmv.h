@@ -225,6 +225,109 @@ SPMV_API spmv_status_t spmv_merge_based_f64(int numRows, int numCols, int nnz,
                                    const double* x, double* y, cudaStream_t stream);
 
 /* ------------------------------------------------------------------ */
+/* CSR5 (src/spmv/csr5/spmv_csr5.cu:13-58, 223-362;                     */
+/* src/formats/sparse_formats.h:284-386).                               */
+/* ------------------------------------------------------------------ */
+/* Tile size getCSR5Config picks for warp 32 (spmv_csr5.cu:13-32): 128. */
+SPMV_API int spmv_csr5_default_sigma(void);
+/* ceil(nnz / sigma). */
+SPMV_API int spmv_csr5_num_tiles(int nnz, int sigma);
+/* csr5_compute_tile_boundaries_kernel (spmv_csr5.cu:36-58): for tile t,
+ * tile_row_ptr[t] = last row r in [0,numRows) with rowPtr[r] <= t*sigma and
+ * tile_nnz_offset[t] = t*sigma - rowPtr[r].  Arrays hold
+ * spmv_csr5_num_tiles() entries (device).  Bit-exact. */
+SPMV_API spmv_status_t spmv_csr5_preprocess(const int* rowPtr, int numRows, int nnz, int sigma,
+                                            int* tile_row_ptr, int* tile_nnz_offset, cudaStream_t stream);
+/* spmv_csr5<T> (spmv_csr5.cu:277-362): SpMV over sigma-nnz tiles described
+ * by the metadata above; y = alpha*A*x + beta*y, no atomics (split rows are
+ * joined by a carry fix-up in tile order).  sigma must be 128 or 256. */
+SPMV_API spmv_status_t spmv_csr5_f32(int numRows, int numCols, int nnz, const int* rowPtr, const int* colIdx,
+                                     const float* values, int sigma, const int* tile_row_ptr,
+                                     const int* tile_nnz_offset, const float* x, float* y, float alpha,
+                                     float beta, const spmv_opts_t* opts);
+SPMV_API spmv_status_t spmv_csr5_f64(int numRows, int numCols, int nnz, const int* rowPtr, const int* colIdx,
+                                     const double* values, int sigma, const int* tile_row_ptr,
+                                     const int* tile_nnz_offset, const double* x, double* y, double alpha,
+                                     double beta, const spmv_opts_t* opts);
+
+/* ------------------------------------------------------------------ */
+/* ELLPACK (src/spmv/ellpack/spmv_ellpack.{cuh,cu}).                    */
+/* ------------------------------------------------------------------ */
+/* Longest row (the width csr_to_ellpack auto-detects,
+ * spmv_ellpack.cu:17-24); *maxLen is host memory. */
+SPMV_API spmv_status_t spmv_max_row_length(const int* rowPtr, int numRows, int* maxLen, cudaStream_t stream);
+/* csr_to_ellpack (spmv_ellpack.cu:11-70) on the device: ellCol/ellVal hold
+ * numRows*width entries, slot (r, i) at r + i*numRows, padding col -1 and
+ * value 0.  Rows longer than width keep their first width entries, as the
+ * reference does; *truncatedRows (host, may be NULL) counts them.
+ * Bit-exact with the reference. */
+SPMV_API spmv_status_t spmv_csr_to_ell_f32(int numRows, int nnz, const int* rowPtr, const int* colIdx,
+                                           const float* values, int width, int* ellCol, float* ellVal,
+                                           long long* truncatedRows, cudaStream_t stream);
+SPMV_API spmv_status_t spmv_csr_to_ell_f64(int numRows, int nnz, const int* rowPtr, const int* colIdx,
+                                           const double* values, int width, int* ellCol, double* ellVal,
+                                           long long* truncatedRows, cudaStream_t stream);
+/* spmv_ellpack<T> (spmv_ellpack.cu:72-91): y = alpha*A*x + beta*y over the
+ * column-major ELL arrays; slots with col < 0 are skipped. */
+SPMV_API spmv_status_t spmv_ellpack_f32(int numRows, int width, const int* ellCol, const float* ellVal,
+                                        const float* x, float* y, float alpha, float beta, cudaStream_t stream);
+SPMV_API spmv_status_t spmv_ellpack_f64(int numRows, int width, const int* ellCol, const double* ellVal,
+                                        const double* x, double* y, double alpha, double beta,
+                                        cudaStream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Reorders (device).  Reference: reorderMatrixByRowLength             */
+/* (tests/test_row_reordering.cu:99-143), restoreOrder                  */
+/* (tests/test_combined_optimizations.cu:176-181), reorderColumns,      */
+/* reorderXVector, sortColumnsWithinRows                                */
+/* (src/preprocessing/column_reorder.cuh:42-201), reorderColumnsRCM and */
+/* reorderColumnsByFrequency (tests/test_column_reordering.cu:116-199). */
+/* ------------------------------------------------------------------ */
+typedef enum {
+    SPMV_COLPERM_CENTER_OF_MASS = 0,  /* key: float mean of the rows touching the column (0 if none),
+                                         summed in row order; ties by column id            */
+    SPMV_COLPERM_MIN_ROW = 1,         /* the reference's "RCM": key = first row touching the column
+                                         (numRows if none); ties by column id               */
+    SPMV_COLPERM_FREQUENCY = 2        /* nonzeros per column, descending; ties by column id  */
+} spmv_colperm_t;
+
+/* Stable sort of rows by length: rowMap[new] = old, newRowPtr (numRows+1),
+ * rows copied in that order.  Bit-exact with std::stable_sort. */
+SPMV_API spmv_status_t spmv_reorder_rows_by_length_f32(int numRows, int nnz, const int* rowPtr, const int* colIdx,
+                                                       const float* values, int* rowMap, int* newRowPtr,
+                                                       int* newColIdx, float* newValues, cudaStream_t stream);
+SPMV_API spmv_status_t spmv_reorder_rows_by_length_f64(int numRows, int nnz, const int* rowPtr, const int* colIdx,
+                                                       const double* values, int* rowMap, int* newRowPtr,
+                                                       int* newColIdx, double* newValues, cudaStream_t stream);
+/* y[rowMap[i]] = yPerm[i]. */
+SPMV_API spmv_status_t spmv_restore_order_f32(int numRows, const float* yPerm, const int* rowMap, float* y,
+                                              cudaStream_t stream);
+SPMV_API spmv_status_t spmv_restore_order_f64(int numRows, const double* yPerm, const int* rowMap, double* y,
+                                              cudaStream_t stream);
+/* Column permutation perm[new] = old (numCols entries).  keys (optional,
+ * device): float per column for CENTER_OF_MASS, int per column otherwise.
+ * The centre-of-mass order is bit-exact with reorderColumns; for MIN_ROW and
+ * FREQUENCY the reference's std::sort leaves tie order unspecified, and
+ * this library breaks ties by ascending column id. */
+SPMV_API spmv_status_t spmv_column_perm(spmv_colperm_t kind, int numRows, int numCols, int nnz,
+                                        const int* rowPtr, const int* colIdx, int* perm, void* keys,
+                                        cudaStream_t stream);
+/* newColIdx[j] = inv[colIdx[j]] with inv[perm[i]] = i. */
+SPMV_API spmv_status_t spmv_apply_column_perm(int numCols, int nnz, const int* perm, const int* colIdx,
+                                              int* newColIdx, cudaStream_t stream);
+/* xr[i] = x[perm[i]] (reorderXVector). */
+SPMV_API spmv_status_t spmv_permute_x_f32(int numCols, const int* perm, const float* x, float* xr,
+                                          cudaStream_t stream);
+SPMV_API spmv_status_t spmv_permute_x_f64(int numCols, const int* perm, const double* x, double* xr,
+                                          cudaStream_t stream);
+/* In place: each row's (column, value) pairs ordered by column, then value
+ * (pair ordering of std::sort on pair<int, T>). */
+SPMV_API spmv_status_t spmv_sort_columns_within_rows_f32(int numRows, int numCols, int nnz, const int* rowPtr,
+                                                         int* colIdx, float* values, cudaStream_t stream);
+SPMV_API spmv_status_t spmv_sort_columns_within_rows_f64(int numRows, int numCols, int nnz, const int* rowPtr,
+                                                         int* colIdx, double* values, cudaStream_t stream);
+
+/* ------------------------------------------------------------------ */
 /* Plans: a matrix plus everything one kernel needs precomputed         */
 /* (tile coordinates, scratch, format copies).  This is the GB300       */
 /* native replacement for spmv_exec<T>(handle, format, matrix, ...)     */

@@ -88,6 +88,26 @@ SIGNATURES = {
     "spmv_merge_path_search": (S, [P, I, I, P, I, P, P, P]),
     "spmv_merge_based_f32": (S, [I, I, I, P, P, P, P, P, P]),
     "spmv_merge_based_f64": (S, [I, I, I, P, P, P, P, P, P]),
+    "spmv_csr5_default_sigma": (I, []),
+    "spmv_csr5_num_tiles": (I, [I, I]),
+    "spmv_csr5_preprocess": (S, [P, I, I, I, P, P, P]),
+    "spmv_csr5_f32": (S, [I, I, I, P, P, P, I, P, P, P, P, F, F, C.POINTER(Opts)]),
+    "spmv_csr5_f64": (S, [I, I, I, P, P, P, I, P, P, P, P, D, D, C.POINTER(Opts)]),
+    "spmv_max_row_length": (S, [P, I, C.POINTER(C.c_int), P]),
+    "spmv_csr_to_ell_f32": (S, [I, I, P, P, P, I, P, P, C.POINTER(C.c_longlong), P]),
+    "spmv_csr_to_ell_f64": (S, [I, I, P, P, P, I, P, P, C.POINTER(C.c_longlong), P]),
+    "spmv_ellpack_f32": (S, [I, I, P, P, P, P, F, F, P]),
+    "spmv_ellpack_f64": (S, [I, I, P, P, P, P, D, D, P]),
+    "spmv_reorder_rows_by_length_f32": (S, [I, I, P, P, P, P, P, P, P, P]),
+    "spmv_reorder_rows_by_length_f64": (S, [I, I, P, P, P, P, P, P, P, P]),
+    "spmv_restore_order_f32": (S, [I, P, P, P, P]),
+    "spmv_restore_order_f64": (S, [I, P, P, P, P]),
+    "spmv_column_perm": (S, [I, I, I, I, P, P, P, P, P]),
+    "spmv_apply_column_perm": (S, [I, I, P, P, P, P]),
+    "spmv_permute_x_f32": (S, [I, P, P, P, P]),
+    "spmv_permute_x_f64": (S, [I, P, P, P, P]),
+    "spmv_sort_columns_within_rows_f32": (S, [I, I, I, P, P, P, P]),
+    "spmv_sort_columns_within_rows_f64": (S, [I, I, I, P, P, P, P]),
     "spmv_plan_create": (S, [C.POINTER(Handle), I, I, I, I, P, P, P, C.POINTER(Variant), C.POINTER(P)]),
     "spmv_plan_destroy": (S, [P]),
     "spmv_plan_get_variant": (S, [P, C.POINTER(Variant)]),

@@ -248,6 +248,144 @@ class Plan:
             pass
 
 
+# ---------------------------------------------------------------------------
+# CSR5 (src/spmv/csr5/spmv_csr5.cuh, src/formats/sparse_formats.h:284-386)
+# ---------------------------------------------------------------------------
+class CSR5Matrix:
+    """CSR5Matrix<T>: borrows the CSR arrays (referenceFromCSR) and owns the
+    tile metadata d_tile_row_ptr / d_tile_nnz_offset (torch int32)."""
+
+    def __init__(self, csr: CSRMatrix):
+        self.csr = csr
+        self.numRows, self.numCols, self.nnz = csr.numRows, csr.numCols, csr.nnz
+        self.sigma = 0
+        self.numTiles = 0
+        self.d_tile_row_ptr = self.d_tile_nnz_offset = None
+
+
+def csr5_preprocess(csr: CSRMatrix, csr5: CSR5Matrix | None = None, sigma: int = 0, stream=None) -> CSR5Matrix:
+    """csr5_preprocess<T> (spmv_csr5.cu:223-275); sigma <= 0 picks the warp-32 default (128)."""
+    torch = _torch()
+    m = csr5 if csr5 is not None else CSR5Matrix(csr)
+    m.sigma = sigma if sigma > 0 else lib().spmv_csr5_default_sigma()
+    m.numTiles = lib().spmv_csr5_num_tiles(csr.nnz, m.sigma)
+    m.d_tile_row_ptr = torch.empty(max(m.numTiles, 1), dtype=torch.int32, device="cuda")
+    m.d_tile_nnz_offset = torch.empty(max(m.numTiles, 1), dtype=torch.int32, device="cuda")
+    check(lib().spmv_csr5_preprocess(_ptr(csr.d_rowPtr), csr.numRows, csr.nnz, m.sigma, _ptr(m.d_tile_row_ptr),
+                                     _ptr(m.d_tile_nnz_offset), _stream_ptr(stream)), "csr5_preprocess")
+    return m
+
+
+def spmv_csr5(m: CSR5Matrix, x, y, alpha=1.0, beta=0.0, opts: Opts | None = None):
+    """spmv_csr5<T> (spmv_csr5.cu:277-362) with alpha/beta applied."""
+    o = opts if opts is not None else spmv_default_opts()
+    A = m.csr
+    f = lib().spmv_csr5_f32 if _is_f32(A) else lib().spmv_csr5_f64
+    check(f(*A.device_args(), m.sigma, _ptr(m.d_tile_row_ptr), _ptr(m.d_tile_nnz_offset), _ptr(x), _ptr(y), alpha,
+            beta, C.byref(o)), "spmv_csr5")
+    return y
+
+
+# ---------------------------------------------------------------------------
+# ELLPACK (src/spmv/ellpack/spmv_ellpack.cuh:26-39)
+# ---------------------------------------------------------------------------
+class ELLPACKMatrix:
+    def __init__(self):
+        self.numRows = self.numCols = self.numElements = self.nnz = 0
+        self.d_colIdx = self.d_values = None
+        self.truncatedRows = 0
+
+
+def max_row_length(A: CSRMatrix, stream=None) -> int:
+    w = C.c_int()
+    check(lib().spmv_max_row_length(_ptr(A.d_rowPtr), A.numRows, C.byref(w), _stream_ptr(stream)), "max_row_length")
+    return w.value
+
+
+def csr_to_ellpack(A: CSRMatrix, ell: ELLPACKMatrix | None = None, maxElements: int = 0, stream=None):
+    """csr_to_ellpack<T> (spmv_ellpack.cu:11-70) on the GPU; maxElements <= 0 = longest row."""
+    torch = _torch()
+    e = ell if ell is not None else ELLPACKMatrix()
+    W = maxElements if maxElements > 0 else max_row_length(A, stream)
+    e.numRows, e.numCols, e.numElements, e.nnz = A.numRows, A.numCols, W, A.nnz
+    tdt = torch.float32 if _is_f32(A) else torch.float64
+    e.d_colIdx = torch.empty(max(A.numRows * W, 1), dtype=torch.int32, device="cuda")
+    e.d_values = torch.empty(max(A.numRows * W, 1), dtype=tdt, device="cuda")
+    t = C.c_longlong()
+    f = lib().spmv_csr_to_ell_f32 if _is_f32(A) else lib().spmv_csr_to_ell_f64
+    check(f(A.numRows, A.nnz, _ptr(A.d_rowPtr), _ptr(A.d_colIdx), _ptr(A.d_values), W, _ptr(e.d_colIdx),
+            _ptr(e.d_values), C.byref(t), _stream_ptr(stream)), "csr_to_ellpack")
+    e.truncatedRows = t.value
+    return e
+
+
+def spmv_ellpack(e: ELLPACKMatrix, x, y, stream=None, alpha=1.0, beta=0.0):
+    """spmv_ellpack<T> (spmv_ellpack.cu:72-91)."""
+    f = lib().spmv_ellpack_f32 if e.d_values.dtype == _torch().float32 else lib().spmv_ellpack_f64
+    check(f(e.numRows, e.numElements, _ptr(e.d_colIdx), _ptr(e.d_values), _ptr(x), _ptr(y), alpha, beta,
+            _stream_ptr(stream)), "spmv_ellpack")
+    return y
+
+
+# ---------------------------------------------------------------------------
+# Reorders
+# ---------------------------------------------------------------------------
+COLPERM_CENTER_OF_MASS, COLPERM_MIN_ROW, COLPERM_FREQUENCY = 0, 1, 2
+
+
+def reorder_rows_by_length(A: CSRMatrix, stream=None):
+    """reorderMatrixByRowLength (tests/test_row_reordering.cu:99-143) on the
+    GPU: returns (rowMap, reordered CSRMatrix with device arrays)."""
+    torch = _torch()
+    rm = torch.empty(max(A.numRows, 1), dtype=torch.int32, device="cuda")
+    B = CSRMatrix(A.rowPtr, A.colIdx, A.values, A.numCols)
+    B.allocateDevice()
+    f = lib().spmv_reorder_rows_by_length_f32 if _is_f32(A) else lib().spmv_reorder_rows_by_length_f64
+    check(f(A.numRows, A.nnz, _ptr(A.d_rowPtr), _ptr(A.d_colIdx), _ptr(A.d_values), _ptr(rm), _ptr(B.d_rowPtr),
+            _ptr(B.d_colIdx), _ptr(B.d_values), _stream_ptr(stream)), "reorder_rows_by_length")
+    return rm[: A.numRows], B
+
+
+def restore_order(y_perm, rowMap, y, stream=None):
+    f = lib().spmv_restore_order_f32 if y.dtype == _torch().float32 else lib().spmv_restore_order_f64
+    check(f(y.numel(), _ptr(y_perm), _ptr(rowMap), _ptr(y), _stream_ptr(stream)), "restore_order")
+    return y
+
+
+def column_perm(A: CSRMatrix, kind: int, stream=None):
+    """(perm new->old, keys) for a column order (see spmv_colperm_t)."""
+    torch = _torch()
+    perm = torch.empty(max(A.numCols, 1), dtype=torch.int32, device="cuda")
+    kdt = torch.float32 if kind == COLPERM_CENTER_OF_MASS else torch.int32
+    keys = torch.empty(max(A.numCols, 1), dtype=kdt, device="cuda")
+    check(lib().spmv_column_perm(kind, A.numRows, A.numCols, A.nnz, _ptr(A.d_rowPtr), _ptr(A.d_colIdx), _ptr(perm),
+                                 _ptr(keys), _stream_ptr(stream)), "column_perm")
+    return perm[: A.numCols], keys[: A.numCols]
+
+
+def apply_column_perm(A: CSRMatrix, perm, stream=None):
+    torch = _torch()
+    out = torch.empty(max(A.nnz, 1), dtype=torch.int32, device="cuda")
+    check(lib().spmv_apply_column_perm(A.numCols, A.nnz, _ptr(perm), _ptr(A.d_colIdx), _ptr(out),
+                                       _stream_ptr(stream)), "apply_column_perm")
+    return out[: A.nnz]
+
+
+def permute_x(perm, x, stream=None):
+    xr = _torch().empty_like(x)
+    f = lib().spmv_permute_x_f32 if x.dtype == _torch().float32 else lib().spmv_permute_x_f64
+    check(f(x.numel(), _ptr(perm), _ptr(x), _ptr(xr), _stream_ptr(stream)), "permute_x")
+    return xr
+
+
+def sort_columns_within_rows(A: CSRMatrix, stream=None):
+    """sortColumnsWithinRows (column_reorder.cuh:175-201), in place on A's device arrays."""
+    f = lib().spmv_sort_columns_within_rows_f32 if _is_f32(A) else lib().spmv_sort_columns_within_rows_f64
+    check(f(A.numRows, A.numCols, A.nnz, _ptr(A.d_rowPtr), _ptr(A.d_colIdx), _ptr(A.d_values), _stream_ptr(stream)),
+          "sort_columns_within_rows")
+    return A
+
+
 def count_distinct_columns(A: CSRMatrix, stream=None) -> int:
     d = C.c_longlong()
     check(lib().spmv_count_distinct_columns(A.numCols, A.nnz, _ptr(A.d_colIdx), C.byref(d), _stream_ptr(stream)),

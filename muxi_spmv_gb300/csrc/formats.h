@@ -1,0 +1,18 @@
+// CSR5 and ELL SpMV launchers (format_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include "kernels.h"
+
+namespace mxs {
+
+// Tile kernel then carry fix-up; carryRow/carryVal hold `tiles` entries.
+template <typename T>
+spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
+                       const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain = nullptr);
+
+template <typename T>
+spmv_status_t run_ell(int numRows, int width, const int* ellCol, const T* ellVal, const T* x, T* y, T alpha, T beta,
+                      cudaStream_t s);
+
+}  // namespace mxs

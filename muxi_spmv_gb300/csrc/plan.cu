@@ -5,6 +5,8 @@
 #include "internal.h"
 #include "kernels.h"
 #include "plan.h"
+#include "formats.h"
+#include "preprocess.h"
 
 namespace mxs {
 
@@ -35,6 +37,7 @@ static spmv_variant_t resolve(const spmv_variant_t* req, int R, int N) {
     if (v.kernel == SPMV_KERNEL_SCALAR) v.threadsPerRow = 1;
     if (v.kernel == SPMV_KERNEL_VECTOR && !v.threadsPerRow) v.threadsPerRow = 32;
     if (v.kernel == SPMV_KERNEL_MERGE && !v.itemsPerThread) v.itemsPerThread = 7;
+    if (v.kernel == SPMV_KERNEL_CSR5 && !v.itemsPerThread) v.itemsPerThread = 4;  // sigma 128
     if (!v.vectorWidth) v.vectorWidth = 1;
     return v;
 }
@@ -75,6 +78,15 @@ static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T
             break;
         case SPMV_KERNEL_MERGE:
             MXS_TRY(run_merge<T>(MergeGeom{v.blockSize, v.itemsPerThread}, p->mergeTiles, p->merge, a, s, evEnd));
+            break;
+        case SPMV_KERNEL_CSR5:
+            MXS_TRY(run_csr5<T>(32 * v.itemsPerThread, p->csr5TileRow, p->csr5Tiles, p->csr5CarryRow,
+                                static_cast<T*>(p->csr5CarryVal), a, s, evEnd));
+            break;
+        case SPMV_KERNEL_ELL:
+            MXS_TRY(run_ell<T>(p->numRows, p->ellWidth, p->ellCol, static_cast<const T*>(p->ellVal), x, y, alpha, beta,
+                               s));
+            if (evEnd) MXS_CUDA(cudaEventRecord(evEnd, s));
             break;
         default:
             MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "plan kernel %d not available", (int)v.kernel);
@@ -140,6 +152,64 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
                 }
             }
         }
+    } else if (v.kernel == SPMV_KERNEL_CSR5) {
+        const int sigma = 32 * v.itemsPerThread;
+        if (sigma != 128 && sigma != 256) {
+            set_error(__FILE__, __LINE__, "CSR5 needs itemsPerThread 4 or 8 (sigma 128 or 256)");
+            st = SPMV_ERROR_INTERNAL;
+        } else if (R > 0 && N > 0) {
+            const long long T = ((long long)N + sigma - 1) / sigma;
+            const size_t a4 = ((sizeof(int) * T) + 255) & ~size_t(255);
+            const size_t bytes = 3 * a4 + vs * T;
+            cudaError_t e = cudaMalloc(&p->csr5Buf, bytes);
+            if (e != cudaSuccess) {
+                set_error(__FILE__, __LINE__, "plan allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+                st = SPMV_ERROR_MEMORY_ALLOC;
+            } else {
+                char* b = static_cast<char*>(p->csr5Buf);
+                p->csr5Tiles = T;
+                p->csr5TileRow = reinterpret_cast<int*>(b);
+                p->csr5TileOff = reinterpret_cast<int*>(b + a4);
+                p->csr5CarryRow = reinterpret_cast<int*>(b + 2 * a4);
+                p->csr5CarryVal = b + 3 * a4;
+                p->workspaceBytes = bytes;
+                st = csr5_tiles(rowPtr, R, N, sigma, p->csr5TileRow, p->csr5TileOff, h->stream);
+                if (st == SPMV_SUCCESS) {
+                    e = cudaStreamSynchronize(h->stream);
+                    if (e != cudaSuccess) st = cuda_fail(e, "plan build", __FILE__, __LINE__);
+                }
+            }
+        }
+    } else if (v.kernel == SPMV_KERNEL_ELL) {
+        int W = 0;
+        st = max_row_length(rowPtr, R, &W, h->stream);
+        // ELL stores rows*width slots; it pays only while padding stays within 2x.
+        if (st == SPMV_SUCCESS && (long long)R * W > 2LL * (N > 0 ? N : 1)) {
+            set_error(__FILE__, __LINE__, "ELL padding %lld slots for %d nonzeros exceeds 2x", (long long)R * W, N);
+            st = SPMV_ERROR_UNSUPPORTED_FORMAT;
+        }
+        if (st == SPMV_SUCCESS && R > 0 && W > 0) {
+            const size_t slots = (size_t)R * W;
+            const size_t a4 = (sizeof(int) * slots + 255) & ~size_t(255);
+            const size_t bytes = a4 + vs * slots;
+            cudaError_t e = cudaMalloc(&p->ellBuf, bytes);
+            if (e != cudaSuccess) {
+                set_error(__FILE__, __LINE__, "plan allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+                st = SPMV_ERROR_MEMORY_ALLOC;
+            } else {
+                p->ellWidth = W;
+                p->ellCol = static_cast<int*>(p->ellBuf);
+                p->ellVal = static_cast<char*>(p->ellBuf) + a4;
+                p->workspaceBytes = bytes;
+                long long trunc = 0;
+                if (type == SPMV_TYPE_FLOAT)
+                    st = csr_to_ell<float>(R, rowPtr, colIdx, static_cast<const float*>(values), W, p->ellCol,
+                                           static_cast<float*>(p->ellVal), &trunc, h->stream);
+                else
+                    st = csr_to_ell<double>(R, rowPtr, colIdx, static_cast<const double*>(values), W, p->ellCol,
+                                            static_cast<double*>(p->ellVal), &trunc, h->stream);
+            }
+        }
     } else if (v.kernel == SPMV_KERNEL_SCALAR || v.kernel == SPMV_KERNEL_VECTOR) {
         if (v.threadsPerRow < 1 || v.threadsPerRow > 32 || (v.threadsPerRow & (v.threadsPerRow - 1))) {
             set_error(__FILE__, __LINE__, "threadsPerRow must be a power of two in [1,32]");
@@ -151,6 +221,8 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
     }
     if (st != SPMV_SUCCESS) {
         if (p->mergeBuf) cudaFree(p->mergeBuf);
+        if (p->csr5Buf) cudaFree(p->csr5Buf);
+        if (p->ellBuf) cudaFree(p->ellBuf);
         delete p;
         return st;
     }
@@ -190,6 +262,8 @@ spmv_status_t spmv_plan_destroy(spmv_plan_t p) {
         cudaEventDestroy(e.second);
     }
     if (p->mergeBuf) cudaFree(p->mergeBuf);
+    if (p->csr5Buf) cudaFree(p->csr5Buf);
+    if (p->ellBuf) cudaFree(p->ellBuf);
     delete p;
     return SPMV_SUCCESS;
 }

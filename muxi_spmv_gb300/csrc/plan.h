@@ -19,6 +19,18 @@ struct spmv_plan_s {
     long long mergeTiles = 0;
     void* mergeBuf = nullptr;  // tile coordinates + carries (cudaMalloc)
     mxs::MergeScratch merge{};
+    // CSR5: sigma = 32 * itemsPerThread; tile rows / offsets / carries
+    long long csr5Tiles = 0;
+    void* csr5Buf = nullptr;
+    int* csr5TileRow = nullptr;
+    int* csr5TileOff = nullptr;
+    int* csr5CarryRow = nullptr;
+    void* csr5CarryVal = nullptr;
+    // ELL: column-major copy of the matrix
+    int ellWidth = 0;
+    void* ellBuf = nullptr;
+    int* ellCol = nullptr;
+    void* ellVal = nullptr;
     size_t workspaceBytes = 0;
     // main-kernel timing (spmv_plan_profile)
     bool profiling = false;

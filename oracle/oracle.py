@@ -5,7 +5,7 @@ import ctypes as C
 
 import numpy as np
 
-from .build import build
+from .build_oracle import build
 
 _lib = None
 
