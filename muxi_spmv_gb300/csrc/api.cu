@@ -127,7 +127,7 @@ static spmv_status_t check_csr_args(int R, int C, int N, const int* rowPtr, cons
     return SPMV_SUCCESS;
 }
 
-const MergeGeom kDefaultMerge = {256, 7};
+const MergeGeom kDefaultMerge = {256, 8, 4};
 
 template <typename T>
 spmv_status_t merge_stateless(const MergeGeom& g, const RowsArgs<T>& a, cudaStream_t s) {
@@ -162,7 +162,7 @@ static spmv_status_t csr_exec(const spmv_variant_t* v, int R, int C, int N, cons
         return finish<T>(opts, s);
     }
     RowsArgs<T> a{R, N, rowPtr, colIdx, values, x, y, alpha, beta, beta == T(0)};
-    spmv_variant_t def{SPMV_KERNEL_MERGE, 256, 0, 7, 1};
+    spmv_variant_t def{SPMV_KERNEL_MERGE, 256, 0, 8, 4};
     if (!v) v = &def;
     switch (v->kernel) {
         case SPMV_KERNEL_SCALAR:
@@ -174,9 +174,8 @@ static spmv_status_t csr_exec(const spmv_variant_t* v, int R, int C, int N, cons
             break;
         case SPMV_KERNEL_MERGE:
         case SPMV_KERNEL_AUTO: {
-            MergeGeom g{v->blockSize ? v->blockSize : 256, v->itemsPerThread ? v->itemsPerThread : 7};
-            if (v->kernel == SPMV_KERNEL_AUTO) g = kDefaultMerge;
-            if (!merge_geom_supported(g.block, g.ipt))
+            MergeGeom g = v->kernel == SPMV_KERNEL_AUTO ? kDefaultMerge : merge_geom_of(*v);
+            if (!merge_geom_supported(g))
                 MXS_FAIL(SPMV_ERROR_INTERNAL, "unsupported merge shape block=%d ipt=%d", g.block, g.ipt);
             MXS_TRY(merge_stateless<T>(g, a, s));
             break;
@@ -306,14 +305,14 @@ spmv_status_t spmv_merge_path_search(const int* rowPtr, int numRows, int nnz, co
 
 spmv_status_t spmv_merge_based_f32(int R, int C, int N, const int* rowPtr, const int* colIdx, const float* values,
                                    const float* x, float* y, cudaStream_t stream) {
-    spmv_variant_t v{SPMV_KERNEL_MERGE, 256, 0, 7, 1};
+    spmv_variant_t v{SPMV_KERNEL_MERGE, 256, 0, 8, 4};
     spmv_opts_t o = spmv_default_opts();
     o.stream = reinterpret_cast<void*>(stream);
     return csr_exec<float>(&v, R, C, N, rowPtr, colIdx, values, x, y, 1.0f, 0.0f, &o);
 }
 spmv_status_t spmv_merge_based_f64(int R, int C, int N, const int* rowPtr, const int* colIdx,
                                    const double* values, const double* x, double* y, cudaStream_t stream) {
-    spmv_variant_t v{SPMV_KERNEL_MERGE, 256, 0, 7, 1};
+    spmv_variant_t v{SPMV_KERNEL_MERGE, 256, 0, 8, 4};
     spmv_opts_t o = spmv_default_opts();
     o.stream = reinterpret_cast<void*>(stream);
     return csr_exec<double>(&v, R, C, N, rowPtr, colIdx, values, x, y, 1.0, 0.0, &o);

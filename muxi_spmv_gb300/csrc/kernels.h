@@ -29,12 +29,19 @@ spmv_status_t run_scale(long long n, T* y, T beta, cudaStream_t s);
 
 // ---- merge path (merge_kernels.cu) ----
 // Merge-path tile geometry for a given block size / items per thread.
+// vec == 0: per-item merge consumer (ipt merge items per thread).
+// vec == 4: nonzero-vectorised consumer (ipt consecutive nonzeros per thread,
+//           16-byte loads); a tile holds block*ipt - 4 merge items so the
+//           16-byte-aligned cover of its nonzeros fits the CTA.
 struct MergeGeom {
     int block;
     int ipt;
-    long long tile() const { return (long long)block * ipt; }
+    int vec = 0;
+    long long tile() const { return (long long)block * ipt - (vec ? 4 : 0); }
 };
-bool merge_geom_supported(int block, int ipt);
+// Builds the geometry of a MERGE variant (defaults filled in).
+MergeGeom merge_geom_of(const spmv_variant_t& v);
+bool merge_geom_supported(const MergeGeom& g);
 // Number of tiles for a matrix: ceil((R+N)/tile), at least 1.
 long long merge_tile_count(int numRows, int nnz, const MergeGeom& g);
 // Bytes of scratch the merge path needs for P tiles and value size vsize:

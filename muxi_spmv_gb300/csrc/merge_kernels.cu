@@ -72,8 +72,18 @@ spmv_status_t merge_search(const int* rowPtr, int numRows, int nnz, const int* d
 // ---------------------------------------------------------------------------
 // Tile geometry and coordinates.
 // ---------------------------------------------------------------------------
-bool merge_geom_supported(int block, int ipt) {
-    return (block == 128 || block == 256) && (ipt == 3 || ipt == 5 || ipt == 7 || ipt == 9 || ipt == 11);
+bool merge_geom_supported(const MergeGeom& g) {
+    if (g.block != 128 && g.block != 256) return false;
+    if (g.vec) return g.vec == 4 && (g.ipt == 4 || g.ipt == 8 || g.ipt == 12 || g.ipt == 16);
+    return g.ipt == 3 || g.ipt == 5 || g.ipt == 7 || g.ipt == 9 || g.ipt == 11;
+}
+
+MergeGeom merge_geom_of(const spmv_variant_t& v) {
+    MergeGeom g;
+    g.block = v.blockSize ? v.blockSize : 256;
+    g.vec = v.vectorWidth == 4 ? 4 : 0;
+    g.ipt = v.itemsPerThread ? v.itemsPerThread : (g.vec ? 8 : 7);
+    return g;
 }
 
 long long merge_tile_count(int numRows, int nnz, const MergeGeom& g) {
@@ -243,6 +253,151 @@ merge_tile_kernel(int numRows, const int* __restrict__ rowPtr, const int* __rest
     }
 }
 
+// ---------------------------------------------------------------------------
+// Tile kernel, nonzero-vectorised consumer.
+//
+// Same tiles, same carries, but the work is laid out by nonzero instead of by
+// merge item: the CTA covers the 16-byte-aligned span [a0, a0 + BLOCK*EPT)
+// with a0 = j0 rounded down to 4 elements, and thread t owns the EPT
+// consecutive positions a0 + t*EPT.. (16-byte loads of colIdx and values,
+// then EPT independent gathers of x).  Only positions in [j0, j1) count.  A
+// thread finds the row of its first nonzero with one binary search in the
+// tile's staged rowPtr slice, walks its nonzeros summing per row, writes the
+// rows that end inside it, and the block scan joins rows that cross threads.
+// Rows that end in this tile but own no nonzero in it (empty rows, or a row
+// whose nonzeros all lie in earlier tiles) get y = beta*y here; the carry
+// fix-up adds their earlier partial sums.
+// ---------------------------------------------------------------------------
+template <typename T, int EPT>
+__device__ __forceinline__ void load_span(const int* __restrict__ colIdx, const T* __restrict__ values,
+                                          const T* __restrict__ x, int nnz, int base, int lo, int hi, T (&p)[EPT]) {
+    if (base + EPT <= nnz) {
+#pragma unroll
+        for (int q = 0; q < EPT; q += 4) {
+            const int4 c = ld_stream4(colIdx + base + q);
+            const Quad<T> v = ld_stream_quad(values + base + q);
+            const int cc[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int j = base + q + e;
+                p[q + e] = (j >= lo && j < hi) ? v.v[e] * ld_x(x + cc[e]) : T(0);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            const int j = base + e;
+            p[e] = (j >= lo && j < hi) ? ld_stream(values + j) * ld_x(x + ld_stream(colIdx + j)) : T(0);
+        }
+    }
+}
+
+template <typename T, int BLOCK, int EPT>
+__global__ void __launch_bounds__(BLOCK)
+merge_vec_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int* __restrict__ colIdx,
+                 const T* __restrict__ values, const T* __restrict__ x, T* __restrict__ y, T alpha, T beta,
+                 int betaZero, const int* __restrict__ tileRow, const int* __restrict__ tileNnz,
+                 int* __restrict__ carryRow, T* __restrict__ carryVal) {
+    constexpr int SPAN = BLOCK * EPT;
+    constexpr int NW = BLOCK / 32;
+    __shared__ int sRp[SPAN];  // rowPtr[r0 .. r1+1]; a tile has at most SPAN-4 row ends
+    __shared__ int sWarpKey[NW];
+    __shared__ T sWarpVal[NW];
+    __shared__ int sKey[BLOCK];
+    __shared__ T sIncl[BLOCK];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long t = blockIdx.x;
+    const int r0 = tileRow[t], j0 = tileNnz[t];
+    const int r1 = tileRow[t + 1], j1 = tileNnz[t + 1];
+    const int nr = r1 - r0;
+    const bool bz = betaZero != 0;
+
+    for (int k = tid; k < nr + 2; k += BLOCK) sRp[k] = __ldg(rowPtr + min(r0 + k, numRows));
+
+    const int base = (j0 & ~3) + tid * EPT;
+    const int lo = max(base, j0), hi = min(base + EPT, j1);
+    const bool has = lo < hi;
+    T p[EPT];
+    if (has) load_span<T, EPT>(colIdx, values, x, nnz, base, lo, hi, p);
+    __syncthreads();
+
+    // Rows ending in this tile without a nonzero in it.
+    for (int k = tid; k < nr; k += BLOCK) {
+        const int first = k == 0 ? j0 : sRp[k];
+        if (sRp[k + 1] <= first) y[r0 + k] = bz ? T(0) : beta * y[r0 + k];
+    }
+
+    int key = 0x7fffffff, startKey = -1, headRow = -1, rowEnd = 0;
+    T run = T(0), headVal = T(0);
+    if (has) {
+        int l = 0, h = nr;  // last local row starting at or before lo
+        while (l < h) {
+            const int m = (l + h + 1) >> 1;
+            if (sRp[m] <= lo) l = m;
+            else h = m - 1;
+        }
+        key = startKey = l;
+        rowEnd = sRp[l + 1];
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            const int q = base + e;
+            if (q >= lo && q < hi) {
+                if (q >= rowEnd) {
+                    if (headRow < 0) {
+                        headRow = key;
+                        headVal = run;
+                    } else {
+                        y[r0 + key] = axpby(alpha, run, beta, bz, y + r0 + key);
+                    }
+                    do {
+                        ++key;
+                        rowEnd = sRp[key + 1];
+                    } while (q >= rowEnd);
+                    run = T(0);
+                }
+                run += p[e];
+            }
+        }
+    }
+
+    // Block-wide inclusive segmented scan of (tail row, partial).
+    T v = run;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int k2 = __shfl_up_sync(kFull, key, off);
+        const T v2 = __shfl_up_sync(kFull, v, off);
+        if (lane >= off && k2 == key) v += v2;
+    }
+    if (lane == 31) {
+        sWarpKey[warp] = key;
+        sWarpVal[warp] = v;
+    }
+    __syncthreads();
+    T pre = T(0);
+    for (int w = warp - 1; w >= 0; --w) {
+        if (sWarpKey[w] != key) break;
+        pre += sWarpVal[w];
+    }
+    v += pre;
+    sKey[tid] = key;
+    sIncl[tid] = v;
+    __syncthreads();
+
+    if (has) {
+        const T cin = (tid > 0 && sKey[tid - 1] == startKey) ? sIncl[tid - 1] : T(0);
+        if (headRow >= 0) y[r0 + headRow] = axpby(alpha, headVal + cin, beta, bz, y + r0 + headRow);
+        if (key < nr && rowEnd == hi) y[r0 + key] = axpby(alpha, v, beta, bz, y + r0 + key);
+        if (hi == j1) {
+            carryRow[t] = r1;
+            carryVal[t] = key == nr ? v : T(0);
+        }
+    } else if (tid == 0 && j1 == j0) {
+        carryRow[t] = r1;
+        carryVal[t] = T(0);
+    }
+}
+
 // Adds the carries of each split row, in tile order, once per row.
 template <typename T>
 __global__ void merge_fixup_kernel(long long P, int numRows, const int* __restrict__ carryRow,
@@ -264,12 +419,39 @@ static void launch_merge(long long P, const MergeScratch& sc, const RowsArgs<T>&
         sc.tileNnz, sc.carryRow, static_cast<T*>(sc.carryVal));
 }
 
+template <typename T, int BLOCK, int EPT>
+static void launch_merge_vec(long long P, const MergeScratch& sc, const RowsArgs<T>& a, cudaStream_t s) {
+    merge_vec_kernel<T, BLOCK, EPT><<<(unsigned)P, BLOCK, 0, s>>>(
+        a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha, a.beta, a.betaZero, sc.tileRow,
+        sc.tileNnz, sc.carryRow, static_cast<T*>(sc.carryVal));
+}
+
 template <typename T>
 spmv_status_t run_merge(const MergeGeom& g, long long P, const MergeScratch& sc, const RowsArgs<T>& a,
                         cudaStream_t s, cudaEvent_t afterMain) {
     if (P > 0x7fffffffLL) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "too many merge tiles");
     bool ok = true;
-    if (g.block == 256) {
+    if (g.vec) {
+        if (g.block == 256) {
+            switch (g.ipt) {
+                case 4: launch_merge_vec<T, 256, 4>(P, sc, a, s); break;
+                case 8: launch_merge_vec<T, 256, 8>(P, sc, a, s); break;
+                case 12: launch_merge_vec<T, 256, 12>(P, sc, a, s); break;
+                case 16: launch_merge_vec<T, 256, 16>(P, sc, a, s); break;
+                default: ok = false;
+            }
+        } else if (g.block == 128) {
+            switch (g.ipt) {
+                case 4: launch_merge_vec<T, 128, 4>(P, sc, a, s); break;
+                case 8: launch_merge_vec<T, 128, 8>(P, sc, a, s); break;
+                case 12: launch_merge_vec<T, 128, 12>(P, sc, a, s); break;
+                case 16: launch_merge_vec<T, 128, 16>(P, sc, a, s); break;
+                default: ok = false;
+            }
+        } else {
+            ok = false;
+        }
+    } else if (g.block == 256) {
         switch (g.ipt) {
             case 3: launch_merge<T, 256, 3>(P, sc, a, s); break;
             case 5: launch_merge<T, 256, 5>(P, sc, a, s); break;

@@ -30,13 +30,13 @@ static spmv_variant_t resolve(const spmv_variant_t* req, int R, int N) {
     if (req) v = *req;
     if (v.kernel == SPMV_KERNEL_HEURISTIC) return heuristic_variant(R, N);
     if (v.kernel == SPMV_KERNEL_AUTO) {
-        v = spmv_variant_t{SPMV_KERNEL_MERGE, 256, 0, 7, 1};
+        v = spmv_variant_t{SPMV_KERNEL_MERGE, 256, 0, 8, 4};
         return v;
     }
     if (!v.blockSize) v.blockSize = 256;
     if (v.kernel == SPMV_KERNEL_SCALAR) v.threadsPerRow = 1;
     if (v.kernel == SPMV_KERNEL_VECTOR && !v.threadsPerRow) v.threadsPerRow = 32;
-    if (v.kernel == SPMV_KERNEL_MERGE && !v.itemsPerThread) v.itemsPerThread = 7;
+    if (v.kernel == SPMV_KERNEL_MERGE && !v.itemsPerThread) v.itemsPerThread = v.vectorWidth == 4 ? 8 : 7;
     if (v.kernel == SPMV_KERNEL_CSR5 && !v.itemsPerThread) v.itemsPerThread = 4;  // sigma 128
     if (!v.vectorWidth) v.vectorWidth = 1;
     return v;
@@ -77,7 +77,7 @@ static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T
             if (evEnd) MXS_CUDA(cudaEventRecord(evEnd, s));
             break;
         case SPMV_KERNEL_MERGE:
-            MXS_TRY(run_merge<T>(MergeGeom{v.blockSize, v.itemsPerThread}, p->mergeTiles, p->merge, a, s, evEnd));
+            MXS_TRY(run_merge<T>(merge_geom_of(v), p->mergeTiles, p->merge, a, s, evEnd));
             break;
         case SPMV_KERNEL_CSR5:
             MXS_TRY(run_csr5<T>(32 * v.itemsPerThread, p->csr5TileRow, p->csr5Tiles, p->csr5CarryRow,
@@ -130,8 +130,8 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
     spmv_status_t st = SPMV_SUCCESS;
     const spmv_variant_t& v = p->variant;
     if (v.kernel == SPMV_KERNEL_MERGE) {
-        MergeGeom g{v.blockSize, v.itemsPerThread};
-        if (!merge_geom_supported(g.block, g.ipt)) {
+        const MergeGeom g = merge_geom_of(v);
+        if (!merge_geom_supported(g)) {
             set_error(__FILE__, __LINE__, "unsupported merge shape block=%d ipt=%d", g.block, g.ipt);
             st = SPMV_ERROR_INTERNAL;
         } else if (R > 0 && N > 0) {

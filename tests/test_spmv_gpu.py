@@ -50,7 +50,9 @@ def cases(mx):
     return build_cases(mx)
 
 
-VARIANTS = [("merge", 3, 256, 7, 0, 1), ("merge", 3, 256, 3, 0, 1), ("merge", 3, 256, 11, 0, 1),
+VARIANTS = [("mvec", 3, 256, 8, 0, 4), ("mvec", 3, 256, 4, 0, 4), ("mvec", 3, 256, 16, 0, 4),
+            ("mvec", 3, 128, 12, 0, 4), ("mvec", 3, 128, 8, 0, 4),
+            ("merge", 3, 256, 7, 0, 1), ("merge", 3, 256, 3, 0, 1), ("merge", 3, 256, 11, 0, 1),
             ("merge", 3, 128, 5, 0, 1), ("merge", 3, 128, 9, 0, 1),
             ("scalar", 1, 256, 0, 1, 1), ("vec2", 2, 256, 0, 2, 1), ("vec4q", 2, 128, 0, 4, 4),
             ("vec8", 2, 512, 0, 8, 1), ("vec8q", 2, 256, 0, 8, 4), ("vec16q", 2, 256, 0, 16, 4),
