@@ -157,6 +157,25 @@ SPMV_API spmv_status_t spmv_csr_f64(int numRows, int numCols, int nnz,
                            const double* x, double* y, double alpha, double beta,
                            const spmv_opts_t* opts);
 
+/* FP32 CSR SpMV that allocates no device memory (no counterpart in the
+ * reference).  Same kernels and results as spmv_csr_f32 (default merge-path
+ * variant), for callers that cannot allocate: code recording a CUDA graph,
+ * code running under a device-memory budget owned by another allocator, or
+ * a real-time loop that must not pay an allocation or the synchronisation it
+ * can cause.  The caller passes inputs and outputs; the scratch (tile
+ * coordinates and carries) is a fixed 8 MiB device array inside the library,
+ * so numRows + nnz may reach about 1.07e9 -- larger matrices are rejected with
+ * SPMV_ERROR_MEMORY_ALLOC and a message.  Every GPU that loads the library
+ * keeps that array until the process exits.  The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress); make it before any
+ * stream capture.  All calls share the one array: calls that can overlap on
+ * the GPU (different streams without ordering) race and must be serialised
+ * by the caller. */
+SPMV_API spmv_status_t spmv_csr_noalloc_f32(int numRows, int numCols, int nnz,
+                                            const int* rowPtr, const int* colIdx, const float* values,
+                                            const float* x, float* y, float alpha, float beta,
+                                            cudaStream_t stream);
+
 /* Kernel variants of the CSR family (the autotuner's search space).
  * Replaces the reference's fixed choice between spmv_csr_scalar_kernel,
  * spmv_csr_vector_kernel and the N-threads-per-row family

@@ -81,6 +81,7 @@ SIGNATURES = {
     "spmv_abi_version": (I, []),
     "spmv_csr_f32": (S, [I, I, I, P, P, P, P, P, F, F, C.POINTER(Opts)]),
     "spmv_csr_f64": (S, [I, I, I, P, P, P, P, P, D, D, C.POINTER(Opts)]),
+    "spmv_csr_noalloc_f32": (S, [I, I, I, P, P, P, P, P, F, F, P]),
     "spmv_csr_variant_f32": (S, [C.POINTER(Variant), I, I, I, P, P, P, P, P, F, F, C.POINTER(Opts)]),
     "spmv_csr_variant_f64": (S, [C.POINTER(Variant), I, I, I, P, P, P, P, P, D, D, C.POINTER(Opts)]),
     "spmv_merge_default_partitions": (I, [I, I]),
