@@ -201,6 +201,7 @@ def gpu_arm(args):
     with torch.cuda.stream(stream):
         plan.exec(x, y)
     stream.synchronize()
+    plan.device_error()  # raises if a bounded pipeline wait gave up
     y_ref, absum = oracle.spmv_ref(rp, ci, v, xh)
     ratio = oracle.row_errors(y.cpu().numpy(), y_ref, absum, 1e-5 if dtype == np.float32 else 1e-13)
     parity = {"rows_checked": int(A.numRows), "max_err_over_bound": float(ratio.max()),
@@ -250,6 +251,7 @@ def gpu_arm(args):
         f1.record(stream)
     torch.cuda.synchronize(dev)
     e2e_ms = f0.elapsed_time(f1) / args.steps
+    plan.device_error()
     clocks.stop()
 
     if ws > 1:

@@ -187,7 +187,10 @@ typedef enum {
     SPMV_KERNEL_MERGE = 3,     /* merge-path CTA tiles + carry fix-up       */
     SPMV_KERNEL_CSR5 = 4,      /* sigma-nnz tiles (CSR5 metadata)           */
     SPMV_KERNEL_ELL = 5,       /* column-major ELLPACK                      */
-    SPMV_KERNEL_HEURISTIC = 6  /* plan: the reference's avgNnz rule, restated */
+    SPMV_KERNEL_HEURISTIC = 6, /* plan: the reference's avgNnz rule, restated */
+    SPMV_KERNEL_BAND = 7       /* CSR5 tiles of 32*itemsPerThread nonzeros in persistent
+                                  CTAs of blockSize threads that keep a sliding shared-
+                                  memory window of x around the diagonal             */
 } spmv_kernel_t;
 
 /* One launch configuration of a kernel family. */
@@ -259,7 +262,7 @@ SPMV_API spmv_status_t spmv_csr5_preprocess(const int* rowPtr, int numRows, int 
                                             int* tile_row_ptr, int* tile_nnz_offset, cudaStream_t stream);
 /* spmv_csr5<T> (spmv_csr5.cu:277-362): SpMV over sigma-nnz tiles described
  * by the metadata above; y = alpha*A*x + beta*y, no atomics (split rows are
- * joined by a carry fix-up in tile order).  sigma must be 128 or 256. */
+ * joined by a carry fix-up in tile order).  sigma must be 128, 256 or 512. */
 SPMV_API spmv_status_t spmv_csr5_f32(int numRows, int numCols, int nnz, const int* rowPtr, const int* colIdx,
                                      const float* values, int sigma, const int* tile_row_ptr,
                                      const int* tile_nnz_offset, const float* x, float* y, float alpha,
@@ -368,6 +371,12 @@ SPMV_API spmv_status_t spmv_plan_exec_f32(spmv_handle_t* handle, spmv_plan_t pla
                                  const float* x, float beta, float* y);
 SPMV_API spmv_status_t spmv_plan_exec_f64(spmv_handle_t* handle, spmv_plan_t plan, double alpha,
                                  const double* x, double beta, double* y);
+
+/* Device-side failure word of a plan.  The pipelined BAND kernel never waits
+ * without a bound: a wait that gives up (about 2 s) raises this word and the
+ * kernel returns.  Synchronises; *code = 0 when clean, else the raised code
+ * (the call then returns SPMV_ERROR_DEVICE and clears the word). */
+SPMV_API spmv_status_t spmv_plan_device_error(spmv_plan_t plan, int* code);
 
 /* Kernel timing on the launching stream (the role of the reference's
  * GpuTimer, src/utils/timer.h:17-47, moved into the plan): while enabled,

@@ -25,7 +25,8 @@ STATUS_NAMES = {
 SPMV_TYPE_FLOAT, SPMV_TYPE_DOUBLE = 0, 1
 SPMV_OP_NORMAL, SPMV_OP_TRANSPOSE = 0, 1
 
-KERNEL_AUTO, KERNEL_SCALAR, KERNEL_VECTOR, KERNEL_MERGE, KERNEL_CSR5, KERNEL_ELL, KERNEL_HEURISTIC = range(7)
+KERNEL_AUTO, KERNEL_SCALAR, KERNEL_VECTOR, KERNEL_MERGE, KERNEL_CSR5, KERNEL_ELL, KERNEL_HEURISTIC, \
+    KERNEL_BAND = range(8)
 
 
 class SpmvError(RuntimeError):
@@ -115,6 +116,7 @@ SIGNATURES = {
     "spmv_plan_get_workspace_bytes": (S, [P, C.POINTER(C.c_size_t)]),
     "spmv_plan_exec_f32": (S, [C.POINTER(Handle), P, F, P, F, P]),
     "spmv_plan_exec_f64": (S, [C.POINTER(Handle), P, D, P, D, P]),
+    "spmv_plan_device_error": (S, [P, C.POINTER(C.c_int)]),
     "spmv_plan_profile": (S, [P, I]),
     "spmv_plan_profile_read": (S, [P, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "spmv_count_distinct_columns": (S, [I, I, P, C.POINTER(C.c_longlong), P]),

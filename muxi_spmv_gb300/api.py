@@ -15,6 +15,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (GenParams, Opts, SpmvError, Variant, check, lib, KERNEL_AUTO, KERNEL_SCALAR,  # noqa: F401
+                   KERNEL_BAND,
                    KERNEL_VECTOR, KERNEL_MERGE, KERNEL_CSR5, KERNEL_ELL, KERNEL_HEURISTIC,
                    SPMV_TYPE_FLOAT, SPMV_TYPE_DOUBLE)
 
@@ -225,6 +226,13 @@ class Plan:
         f = lib().spmv_plan_exec_f32 if _is_f32(self.A) else lib().spmv_plan_exec_f64
         check(f(self.handle.raw, self._p, alpha, _ptr(x), beta, _ptr(y)), "spmv_plan_exec")
         return y
+
+    def device_error(self) -> int:
+        """Device failure word of the plan's pipelined kernel (0 = clean);
+        raises SpmvError when it is set."""
+        code = C.c_int()
+        check(lib().spmv_plan_device_error(self._p, C.byref(code)), "spmv_plan_device_error")
+        return code.value
 
     def profile(self, enable: bool = True):
         """Records CUDA events around the main kernel of every exec."""

@@ -21,108 +21,24 @@
 #include "device.cuh"
 #include "kernels.h"
 #include "formats.h"
+#include "csr5_tile.cuh"
 
 namespace mxs {
 
-template <typename T, int SIGMA>
+template <typename T, int E>
 __global__ void __launch_bounds__(256)
 csr5_tile_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int* __restrict__ colIdx,
                  const T* __restrict__ values, const T* __restrict__ x, T* __restrict__ y, T alpha, T beta,
                  int betaZero, const int* __restrict__ tileRow, long long tiles, int* __restrict__ carryRow,
                  T* __restrict__ carryVal) {
-    constexpr int E = SIGMA / 32;
+    __shared__ int sRp[8][csr5_rp_cap<E>()];
     const long long t = ((long long)blockIdx.x * 256 + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (t >= tiles) return;  // uniform per warp
-    const bool bz = betaZero != 0;
-    const long long tStart = t * SIGMA;
-    const long long tEnd = tStart + SIGMA < nnz ? tStart + SIGMA : nnz;
-    const int rFirst = tileRow[t];
-    const int rLast = t + 1 < tiles ? tileRow[t + 1] : numRows - 1;
-
-    // Empty rows of this tile's range: (rFirst, rLast], plus leading rows for tile 0.
-    {
-        const int lo = t == 0 ? 0 : rFirst + 1;
-        for (int r = lo + lane; r <= rLast; r += 32)
-            if (__ldg(rowPtr + r) == __ldg(rowPtr + r + 1)) y[r] = bz ? T(0) : beta * y[r];
-    }
-
-    const long long j0 = tStart + (long long)lane * E;
-    const long long laneEnd = j0 + E < tEnd ? j0 + E : tEnd;
-    const bool has = j0 < tEnd;
-
-    int key = 0x7fffffff;  // lanes without elements sort last in the scan
-    T run = T(0), headVal = T(0);
-    int headRow = -1, startRow = -1;
-    long long rowEnd = 0;
-    if (has) {
-        int lo = rFirst, hi = rLast;  // last row with rowPtr <= j0
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (__ldg(rowPtr + mid) <= j0) lo = mid;
-            else hi = mid - 1;
-        }
-        key = startRow = lo;
-        rowEnd = __ldg(rowPtr + lo + 1);
-        T p[E];
-        if (j0 + E <= nnz) {
-#pragma unroll
-            for (int q = 0; q < E; q += 4) {
-                const int4 c = ld_stream4(colIdx + j0 + q);
-                const Quad<T> v = ld_stream_quad(values + j0 + q);
-                p[q + 0] = v.v[0] * ld_x(x + c.x);
-                p[q + 1] = v.v[1] * ld_x(x + c.y);
-                p[q + 2] = v.v[2] * ld_x(x + c.z);
-                p[q + 3] = v.v[3] * ld_x(x + c.w);
-            }
-        } else {
-#pragma unroll
-            for (int e = 0; e < E; ++e)
-                p[e] = j0 + e < tEnd ? ld_stream(values + j0 + e) * ld_x(x + ld_stream(colIdx + j0 + e)) : T(0);
-        }
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const long long j = j0 + e;
-            if (j < laneEnd) {
-                if (j >= rowEnd) {
-                    // `key` is complete; rows skipped on the way are empty.
-                    if (headRow < 0) {
-                        headRow = key;
-                        headVal = run;
-                    } else {
-                        y[key] = axpby(alpha, run, beta, bz, y + key);
-                    }
-                    do {
-                        ++key;
-                        rowEnd = __ldg(rowPtr + key + 1);
-                    } while (j >= rowEnd);
-                    run = T(0);
-                }
-                run += p[e];
-            }
-        }
-    }
-
-    // Segmented inclusive scan over lanes of (tail row, partial).
-    T incl = run;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        const int k2 = __shfl_up_sync(kFull, key, off);
-        const T v2 = __shfl_up_sync(kFull, incl, off);
-        if (lane >= off && k2 == key) incl += v2;
-    }
-    const int prevKey = __shfl_up_sync(kFull, key, 1);
-    const T prevIncl = __shfl_up_sync(kFull, incl, 1);
-    if (!has) return;
-    const T cin = (lane > 0 && prevKey == startRow) ? prevIncl : T(0);
-    if (headRow >= 0) y[headRow] = axpby(alpha, headVal + cin, beta, bz, y + headRow);
-    if (rowEnd == laneEnd) {
-        y[key] = axpby(alpha, incl, beta, bz, y + key);  // tail row ends in this lane
-    }
-    if (laneEnd == tEnd) {  // the lane holding the tile's last nonzero
-        carryRow[t] = rowEnd > laneEnd ? key : -1;
-        carryVal[t] = incl;
-    }
+    Csr5Load<T, E> L;
+    csr5_load<T, E>(L, t, lane, nnz, tiles, numRows, tileRow, rowPtr, colIdx, values);
+    csr5_compute<T, E>(L, t, lane, numRows, nnz, rowPtr, y, alpha, beta, betaZero != 0, carryRow, carryVal,
+                       sRp[threadIdx.x >> 5], [x](int c) { return ld_x(x + c); });
 }
 
 // Adds each split row's carries in tile order (rows with carry -1 skipped).
@@ -144,20 +60,33 @@ spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carr
                        const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain) {
     const unsigned g = grid_for(tiles * 32, 256);
     if (sigma == 128) {
-        csr5_tile_kernel<T, 128><<<g, 256, 0, s>>>(a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha,
-                                                   a.beta, a.betaZero, tileRow, tiles, carryRow, carryVal);
+        csr5_tile_kernel<T, 4><<<g, 256, 0, s>>>(a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha,
+                                                 a.beta, a.betaZero, tileRow, tiles, carryRow, carryVal);
     } else if (sigma == 256) {
-        csr5_tile_kernel<T, 256><<<g, 256, 0, s>>>(a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha,
-                                                   a.beta, a.betaZero, tileRow, tiles, carryRow, carryVal);
+        csr5_tile_kernel<T, 8><<<g, 256, 0, s>>>(a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha,
+                                                 a.beta, a.betaZero, tileRow, tiles, carryRow, carryVal);
+    } else if (sigma == 512) {
+        csr5_tile_kernel<T, 16><<<g, 256, 0, s>>>(a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha,
+                                                  a.beta, a.betaZero, tileRow, tiles, carryRow, carryVal);
     } else {
-        MXS_FAIL(SPMV_ERROR_INTERNAL, "CSR5 sigma must be 128 or 256 (got %d)", sigma);
+        MXS_FAIL(SPMV_ERROR_INTERNAL, "CSR5 sigma must be 128, 256 or 512 (got %d)", sigma);
     }
     MXS_LAUNCH_CHECK();
     if (afterMain) MXS_CUDA(cudaEventRecord(afterMain, s));
+    return run_csr5_fixup<T>(tiles, carryRow, carryVal, a, s);
+}
+
+template <typename T>
+spmv_status_t run_csr5_fixup(long long tiles, const int* carryRow, const T* carryVal, const RowsArgs<T>& a,
+                             cudaStream_t s) {
     csr5_fixup_kernel<T><<<grid_for(tiles, 256), 256, 0, s>>>(tiles, carryRow, carryVal, a.y, a.alpha);
     MXS_LAUNCH_CHECK();
     return SPMV_SUCCESS;
 }
+template spmv_status_t run_csr5_fixup<float>(long long, const int*, const float*, const RowsArgs<float>&,
+                                             cudaStream_t);
+template spmv_status_t run_csr5_fixup<double>(long long, const int*, const double*, const RowsArgs<double>&,
+                                              cudaStream_t);
 template spmv_status_t run_csr5<float>(int, const int*, long long, int*, float*, const RowsArgs<float>&,
                                        cudaStream_t, cudaEvent_t);
 template spmv_status_t run_csr5<double>(int, const int*, long long, int*, double*, const RowsArgs<double>&,

@@ -11,6 +11,11 @@ template <typename T>
 spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
                        const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain = nullptr);
 
+// Adds the carries of rows split between CSR5 tiles, in tile order.
+template <typename T>
+spmv_status_t run_csr5_fixup(long long tiles, const int* carryRow, const T* carryVal, const RowsArgs<T>& a,
+                             cudaStream_t s);
+
 template <typename T>
 spmv_status_t run_ell(int numRows, int width, const int* ellCol, const T* ellVal, const T* x, T* y, T alpha, T beta,
                       cudaStream_t s);

@@ -13,7 +13,8 @@ static spmv_status_t csr5_exec(int R, int C, int N, const int* rowPtr, const int
     clear_error();
     (void)tileOff;  // the kernel needs only the tile start rows
     if (R < 0 || C < 0 || N < 0) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "negative dimension");
-    if (sigma != 128 && sigma != 256) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "sigma must be 128 or 256 (got %d)", sigma);
+    if (sigma != 128 && sigma != 256 && sigma != 512)
+        MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "sigma must be 128, 256 or 512 (got %d)", sigma);
     if (R > 0 && !y) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "y is NULL");
     const cudaStream_t s = opts_stream(opts);
     if (R == 0) return SPMV_SUCCESS;
@@ -22,6 +23,8 @@ static spmv_status_t csr5_exec(int R, int C, int N, const int* rowPtr, const int
     } else {
         if (!rowPtr || !colIdx || !values || !tileRow) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "NULL CSR5 array");
         if (!x) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "x is NULL");
+        if (N > 0x7fffffff - 32768)
+            MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "CSR5 tiles need nnz <= 2^31 - 32769 (got %d)", N);
         const long long tiles = ((long long)N + sigma - 1) / sigma;
         void* buf = nullptr;
         MXS_TRY(scratch_alloc(&buf, (sizeof(int) + sizeof(T)) * tiles + 256, s));

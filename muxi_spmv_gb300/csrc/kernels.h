@@ -66,6 +66,20 @@ template <typename T>
 spmv_status_t run_merge(const MergeGeom& g, long long P, const MergeScratch& sc, const RowsArgs<T>& a,
                         cudaStream_t s, cudaEvent_t afterMain = nullptr);
 
+// Carry fix-up of a merge-path launch (adds carries of split rows in tile order).
+template <typename T>
+spmv_status_t run_merge_fixup(long long P, const MergeScratch& sc, const RowsArgs<T>& a, cudaStream_t s);
+
+// Bulk-copy-pipelined CSR5-tile kernel over a shared-memory x window
+// (band_kernels.cu).  E = nonzeros per lane (4, 8), block = consumer threads
+// (128, 256); tileRow holds the CSR5 tile rows for sigma = 32*E; carries as
+// run_csr5.  errFlag: device int raised (non-zero) if a pipeline wait gave up.
+bool band_shape_supported(int block, int E);
+template <typename T>
+spmv_status_t run_band(int block, int E, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
+                       int* errFlag, const RowsArgs<T>& a, int numCols, cudaStream_t s,
+                       cudaEvent_t afterMain = nullptr);
+
 // Reference-compatible partitioning (spmv_csr5.cu:912-925) and search (:497-533).
 spmv_status_t merge_partitions(int numRows, int nnz, int P, int* pos, cudaStream_t s);
 spmv_status_t merge_search(const int* rowPtr, int numRows, int nnz, const int* diag, int count,

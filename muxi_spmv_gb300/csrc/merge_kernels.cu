@@ -475,11 +475,19 @@ spmv_status_t run_merge(const MergeGeom& g, long long P, const MergeScratch& sc,
     if (!ok) MXS_FAIL(SPMV_ERROR_INTERNAL, "unsupported merge shape block=%d ipt=%d", g.block, g.ipt);
     MXS_LAUNCH_CHECK();
     if (afterMain) MXS_CUDA(cudaEventRecord(afterMain, s));
+    return run_merge_fixup<T>(P, sc, a, s);
+}
+
+template <typename T>
+spmv_status_t run_merge_fixup(long long P, const MergeScratch& sc, const RowsArgs<T>& a, cudaStream_t s) {
     merge_fixup_kernel<T><<<grid_for(P, 256), 256, 0, s>>>(P, a.numRows, sc.carryRow,
                                                           static_cast<const T*>(sc.carryVal), a.y, a.alpha);
     MXS_LAUNCH_CHECK();
     return SPMV_SUCCESS;
 }
+template spmv_status_t run_merge_fixup<float>(long long, const MergeScratch&, const RowsArgs<float>&, cudaStream_t);
+template spmv_status_t run_merge_fixup<double>(long long, const MergeScratch&, const RowsArgs<double>&,
+                                               cudaStream_t);
 
 template spmv_status_t run_merge<float>(const MergeGeom&, long long, const MergeScratch&,
                                         const RowsArgs<float>&, cudaStream_t, cudaEvent_t);

@@ -30,13 +30,17 @@ static spmv_variant_t resolve(const spmv_variant_t* req, int R, int N) {
     if (req) v = *req;
     if (v.kernel == SPMV_KERNEL_HEURISTIC) return heuristic_variant(R, N);
     if (v.kernel == SPMV_KERNEL_AUTO) {
-        v = spmv_variant_t{SPMV_KERNEL_MERGE, 256, 0, 8, 4};
-        return v;
+        // Without a selector model: CSR5 tiles of 256 nonzeros (nnz-balanced,
+        // warp-local, the fastest measured variant on irregular matrices);
+        // merge-path tiles when the nonzero count is beyond CSR5's range.
+        if (N > 0x7fffffff - 32768) return spmv_variant_t{SPMV_KERNEL_MERGE, 256, 0, 8, 4};
+        return spmv_variant_t{SPMV_KERNEL_CSR5, 256, 0, 8, 1};
     }
     if (!v.blockSize) v.blockSize = 256;
     if (v.kernel == SPMV_KERNEL_SCALAR) v.threadsPerRow = 1;
     if (v.kernel == SPMV_KERNEL_VECTOR && !v.threadsPerRow) v.threadsPerRow = 32;
     if (v.kernel == SPMV_KERNEL_MERGE && !v.itemsPerThread) v.itemsPerThread = v.vectorWidth == 4 ? 8 : 7;
+    if (v.kernel == SPMV_KERNEL_BAND && !v.itemsPerThread) v.itemsPerThread = 8;
     if (v.kernel == SPMV_KERNEL_CSR5 && !v.itemsPerThread) v.itemsPerThread = 4;  // sigma 128
     if (!v.vectorWidth) v.vectorWidth = 1;
     return v;
@@ -78,6 +82,10 @@ static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T
             break;
         case SPMV_KERNEL_MERGE:
             MXS_TRY(run_merge<T>(merge_geom_of(v), p->mergeTiles, p->merge, a, s, evEnd));
+            break;
+        case SPMV_KERNEL_BAND:
+            MXS_TRY(run_band<T>(v.blockSize, v.itemsPerThread, p->csr5TileRow, p->csr5Tiles, p->csr5CarryRow,
+                                static_cast<T*>(p->csr5CarryVal), p->errFlag, a, p->numCols, s, evEnd));
             break;
         case SPMV_KERNEL_CSR5:
             MXS_TRY(run_csr5<T>(32 * v.itemsPerThread, p->csr5TileRow, p->csr5Tiles, p->csr5CarryRow,
@@ -152,15 +160,22 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
                 }
             }
         }
-    } else if (v.kernel == SPMV_KERNEL_CSR5) {
+    } else if (v.kernel == SPMV_KERNEL_CSR5 || v.kernel == SPMV_KERNEL_BAND) {
         const int sigma = 32 * v.itemsPerThread;
-        if (sigma != 128 && sigma != 256) {
-            set_error(__FILE__, __LINE__, "CSR5 needs itemsPerThread 4 or 8 (sigma 128 or 256)");
+        if (v.kernel == SPMV_KERNEL_BAND && !band_shape_supported(v.blockSize, v.itemsPerThread)) {
+            set_error(__FILE__, __LINE__, "unsupported band shape block=%d ept=%d", v.blockSize, v.itemsPerThread);
             st = SPMV_ERROR_INTERNAL;
+        } else if (sigma != 128 && sigma != 256 && sigma != 512) {
+            set_error(__FILE__, __LINE__, "CSR5 needs itemsPerThread 4, 8 or 16 (sigma 128, 256 or 512)");
+            st = SPMV_ERROR_INTERNAL;
+        } else if (N > 0x7fffffff - 32768) {
+            set_error(__FILE__, __LINE__, "CSR5 tiles need nnz <= 2^31 - 32769 (got %d)", N);
+            st = SPMV_ERROR_INVALID_MATRIX;
         } else if (R > 0 && N > 0) {
             const long long T = ((long long)N + sigma - 1) / sigma;
             const size_t a4 = ((sizeof(int) * T) + 255) & ~size_t(255);
-            const size_t bytes = 3 * a4 + vs * T;
+            const size_t av = ((vs * T) + 255) & ~size_t(255);
+            const size_t bytes = 3 * a4 + av + 256;  // + the device error word
             cudaError_t e = cudaMalloc(&p->csr5Buf, bytes);
             if (e != cudaSuccess) {
                 set_error(__FILE__, __LINE__, "plan allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
@@ -172,8 +187,11 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
                 p->csr5TileOff = reinterpret_cast<int*>(b + a4);
                 p->csr5CarryRow = reinterpret_cast<int*>(b + 2 * a4);
                 p->csr5CarryVal = b + 3 * a4;
+                p->errFlag = reinterpret_cast<int*>(b + 3 * a4 + av);
                 p->workspaceBytes = bytes;
-                st = csr5_tiles(rowPtr, R, N, sigma, p->csr5TileRow, p->csr5TileOff, h->stream);
+                e = cudaMemsetAsync(p->errFlag, 0, sizeof(int), h->stream);
+                st = e == cudaSuccess ? csr5_tiles(rowPtr, R, N, sigma, p->csr5TileRow, p->csr5TileOff, h->stream)
+                                      : cuda_fail(e, "plan build", __FILE__, __LINE__);
                 if (st == SPMV_SUCCESS) {
                     e = cudaStreamSynchronize(h->stream);
                     if (e != cudaSuccess) st = cuda_fail(e, "plan build", __FILE__, __LINE__);
@@ -227,6 +245,21 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
         return st;
     }
     *out = p;
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_plan_device_error(spmv_plan_t p, int* code) {
+    clear_error();
+    if (!p || !code) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "NULL argument");
+    *code = 0;
+    if (!p->errFlag) return SPMV_SUCCESS;
+    int h = 0;
+    MXS_CUDA(cudaMemcpy(&h, p->errFlag, sizeof(int), cudaMemcpyDeviceToHost));
+    *code = h;
+    if (h) {
+        MXS_CUDA(cudaMemset(p->errFlag, 0, sizeof(int)));
+        MXS_FAIL(SPMV_ERROR_DEVICE, "a pipelined SpMV kernel gave up waiting (code %d); its output is invalid", h);
+    }
     return SPMV_SUCCESS;
 }
 

@@ -26,6 +26,7 @@ struct spmv_plan_s {
     int* csr5TileOff = nullptr;
     int* csr5CarryRow = nullptr;
     void* csr5CarryVal = nullptr;
+    int* errFlag = nullptr;  // device word raised by a pipelined kernel whose wait gave up
     // ELL: column-major copy of the matrix
     int ellWidth = 0;
     void* ellBuf = nullptr;

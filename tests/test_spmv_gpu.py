@@ -95,6 +95,32 @@ def test_variants_match_oracle(mx, cuda, cases, var, dtype):
             check(y, y0, A, xh, alpha, beta)
 
 
+PLAN_VARIANTS = [("band", 7, 256, 8), ("band", 7, 256, 4), ("band", 7, 512, 8), ("band", 7, 512, 4),
+                 ("csr5_512", 4, 256, 16), ("csr5_128", 4, 256, 4)]
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+@pytest.mark.parametrize("var", PLAN_VARIANTS, ids=[f"{v[0]}b{v[2]}e{v[3]}" for v in PLAN_VARIANTS])
+def test_plan_variants_match_oracle(mx, cuda, handle, cases, var, dtype):
+    """Plan-only kernels (tile metadata built at plan creation): the windowed
+    persistent kernel and CSR5 at every tile size, on every edge case."""
+    torch = cuda
+    name_, kernel, block, ept = var
+    for name, (rp, ci, v, cols) in cases.items():
+        A = device_csr(mx, rp, ci, v.astype(dtype), cols)
+        xh = mx.gen_vector(cols, 77, dtype=dtype)
+        x = torch.from_numpy(xh).cuda()
+        p = mx.Plan(handle, A, mx.make_variant(kernel, block, 0, ept, 4))
+        for alpha, beta in ((1.0, 0.0), (-0.5, 2.0)):
+            y0 = mx.gen_vector(A.numRows, 99, dtype=dtype)
+            y = torch.from_numpy(y0.copy()).cuda()
+            p.exec(x, y, alpha, beta)
+            torch.cuda.synchronize()
+            assert p.device_error() == 0
+            check(y, y0, A, xh, alpha, beta)
+        p.destroy()
+
+
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
 def test_stateless_and_merge_based(mx, cuda, cases, dtype):
     torch = cuda
