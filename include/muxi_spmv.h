@@ -448,6 +448,102 @@ SPMV_API spmv_status_t spmv_gen_vector_f32(long long n, unsigned long long seed,
 SPMV_API spmv_status_t spmv_gen_vector_f64(long long n, unsigned long long seed, double lo, double hi,
                                   double* out, int threads);
 
+/* Device-side generators for corpora and batches: same length laws as the
+ * host generators for SPMV_GEN_POISSON_UNIFORM, SPMV_GEN_ZIPF_UNIFORM,
+ * SPMV_GEN_BANDED and SPMV_GEN_BLOCKDIAG, drawn on the GPU (values differ
+ * from the host generators').  Columns are sorted within a row and may
+ * repeat where a row is dense in its range.  All pointers are device
+ * pointers; spmv_gen_device_row_ptr synchronises the stream to read nnz and
+ * fails with SPMV_ERROR_INVALID_MATRIX when nnz >= 2^31. */
+SPMV_API spmv_status_t spmv_gen_device_row_ptr(const spmv_gen_params_t* p, int* rowPtr, long long* nnz,
+                                               cudaStream_t stream);
+SPMV_API spmv_status_t spmv_gen_device_fill_f32(const spmv_gen_params_t* p, const int* rowPtr, int* colIdx,
+                                                float* values, cudaStream_t stream);
+SPMV_API spmv_status_t spmv_gen_device_vector_f32(long long n, unsigned long long seed, double lo, double hi,
+                                                  float* out, cudaStream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Kernel selection.  The reference selects by a fixed rule on the     */
+/* integer mean row length (src/spmv/csr/spmv_csr.cu:115-153, exposed  */
+/* here as SPMV_KERNEL_HEURISTIC); this library adds an exhaustive     */
+/* autotuner over a fixed variant space and a learned selector (an MLP  */
+/* over matrix features, trained on the autotuner's timings).          */
+/* ------------------------------------------------------------------ */
+#define SPMV_NUM_FEATURES 32
+
+/* Writes SPMV_NUM_FEATURES floats describing a device CSR matrix to the
+ * DEVICE buffer `features` (asynchronous on `stream`).  Reads rowPtr in
+ * full and the columns of at most 4096 sampled rows. */
+SPMV_API spmv_status_t spmv_matrix_features(spmv_type_t type, int numRows, int numCols, int nnz,
+                                            const int* rowPtr, const int* colIdx, float* features,
+                                            cudaStream_t stream);
+
+/* Copies the variant search space (at most `capacity` entries) to `out`
+ * and returns its size; out may be NULL to query the size.  The order is
+ * fixed: a selector model's outputs index it. */
+SPMV_API int spmv_variant_space(spmv_variant_t* out, int capacity);
+
+/* Times every candidate (the whole space when candidates is NULL) as a
+ * plan on this matrix: one warm-up, then `repeats` executions (repeats <= 0:
+ * as many as fill about 2 ms, 3 to 500), on the handle's stream.  Variants
+ * whose warm-up is 20x slower than the best so far keep the warm-up time.
+ * msOut[i] = mean milliseconds, or -1 where the variant does not apply
+ * (plan creation refused it); *bestIndex = the fastest. */
+SPMV_API spmv_status_t spmv_autotune(spmv_handle_t* handle, spmv_type_t type, int numRows, int numCols, int nnz,
+                                     const int* rowPtr, const int* colIdx, const void* values,
+                                     const spmv_variant_t* candidates, int numCandidates, int repeats,
+                                     float* msOut, int* bestIndex);
+
+/* Selector network: in -> h1 -> h2 -> out, ReLU, trained on the GPU with
+ * Adam on a masked mean squared error.  X, T, M, Y are DEVICE row-major
+ * [batch x in] / [batch x out] arrays; inputs are standardised with the
+ * model's mean/std before the first layer.  Parameters are laid out
+ * W1[h1 x in], b1, W2[h2 x h1], b2, W3[out x h2], b3. */
+typedef struct spmv_mlp_s* spmv_mlp_t;
+SPMV_API spmv_status_t spmv_mlp_create(int in, int h1, int h2, int out, unsigned long long seed,
+                                       spmv_mlp_t* model);
+SPMV_API spmv_status_t spmv_mlp_destroy(spmv_mlp_t model);
+SPMV_API int spmv_mlp_num_params(spmv_mlp_t model);
+SPMV_API spmv_status_t spmv_mlp_shape(spmv_mlp_t model, int* in, int* h1, int* h2, int* out);
+SPMV_API spmv_status_t spmv_mlp_get_params(spmv_mlp_t model, float* host, int count);
+SPMV_API spmv_status_t spmv_mlp_set_params(spmv_mlp_t model, const float* host, int count);
+/* Host arrays of `in` floats; std entries below 1e-6 are taken as 1. */
+SPMV_API spmv_status_t spmv_mlp_set_normalization(spmv_mlp_t model, const float* mean, const float* std);
+SPMV_API spmv_status_t spmv_mlp_forward(spmv_mlp_t model, const float* X, float* Y, int batch,
+                                        cudaStream_t stream);
+/* Loss and gradients of one batch without updating the model; grads is a
+ * HOST array of spmv_mlp_num_params floats (may be NULL). Synchronises. */
+SPMV_API spmv_status_t spmv_mlp_gradients(spmv_mlp_t model, const float* X, const float* T, const float* M,
+                                          int batch, float* loss, float* grads, cudaStream_t stream);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) at learning rate lr;
+ * *loss (if not NULL) receives the batch loss before the step. */
+SPMV_API spmv_status_t spmv_mlp_train_step(spmv_mlp_t model, const float* X, const float* T, const float* M,
+                                           int batch, float lr, float* loss, cudaStream_t stream);
+/* Model file: magic, version, layer sizes, parameters, normalisation and
+ * a 64-bit checksum; loading verifies all of them. */
+SPMV_API spmv_status_t spmv_mlp_save(spmv_mlp_t model, const char* path);
+SPMV_API spmv_status_t spmv_mlp_load(const char* path, spmv_mlp_t* model);
+
+typedef enum {
+    SPMV_SELECT_HEURISTIC = 0,     /* the reference's mean-row-length rule      */
+    SPMV_SELECT_LEARNED = 1,       /* features + MLP, argmin of predictions     */
+    SPMV_SELECT_AUTOTUNE = 2,      /* time the whole space                      */
+    SPMV_SELECT_LEARNED_TOPK = 3   /* time only the model's topK best guesses   */
+} spmv_select_mode_t;
+
+/* Picks a variant for a device CSR matrix.  `model` is needed by the
+ * learned modes, `values` by the timing modes.  *spaceIndex = index into
+ * spmv_variant_space (-1 when the heuristic's pick is not in the space).
+ * Learned modes never return a variant that plan creation would refuse
+ * (ELL over 2x padding, unsupported shapes). */
+SPMV_API spmv_status_t spmv_select(spmv_handle_t* handle, spmv_select_mode_t mode, spmv_mlp_t model, int topK,
+                                   spmv_type_t type, int numRows, int numCols, int nnz, const int* rowPtr,
+                                   const int* colIdx, const void* values, spmv_variant_t* out, int* spaceIndex);
+/* Registers (model != NULL) or clears a selector model on the handle: plans
+ * created with SPMV_KERNEL_AUTO then take the learned pick.  The handle
+ * borrows the model; it must outlive the handle's use of it. */
+SPMV_API spmv_status_t spmv_set_selector(spmv_handle_t* handle, spmv_mlp_t model);
+
 #ifdef __cplusplus
 }
 #endif

@@ -126,7 +126,30 @@ SIGNATURES = {
     "spmv_gen_fill_f64": (S, [C.POINTER(GenParams), P, P, P]),
     "spmv_gen_vector_f32": (S, [C.c_longlong, C.c_ulonglong, D, D, P, I]),
     "spmv_gen_vector_f64": (S, [C.c_longlong, C.c_ulonglong, D, D, P, I]),
+    "spmv_gen_device_row_ptr": (S, [C.POINTER(GenParams), P, C.POINTER(C.c_longlong), P]),
+    "spmv_gen_device_fill_f32": (S, [C.POINTER(GenParams), P, P, P, P]),
+    "spmv_gen_device_vector_f32": (S, [C.c_longlong, C.c_ulonglong, D, D, P, P]),
+    "spmv_matrix_features": (S, [I, I, I, I, P, P, P, P]),
+    "spmv_variant_space": (I, [P, I]),
+    "spmv_autotune": (S, [C.POINTER(Handle), I, I, I, I, P, P, P, P, I, I, P, C.POINTER(C.c_int)]),
+    "spmv_mlp_create": (S, [I, I, I, I, C.c_ulonglong, C.POINTER(P)]),
+    "spmv_mlp_destroy": (S, [P]),
+    "spmv_mlp_num_params": (I, [P]),
+    "spmv_mlp_shape": (S, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "spmv_mlp_get_params": (S, [P, P, I]),
+    "spmv_mlp_set_params": (S, [P, P, I]),
+    "spmv_mlp_set_normalization": (S, [P, P, P]),
+    "spmv_mlp_forward": (S, [P, P, P, I, P]),
+    "spmv_mlp_gradients": (S, [P, P, P, P, I, C.POINTER(F), P, P]),
+    "spmv_mlp_train_step": (S, [P, P, P, P, I, F, C.POINTER(F), P]),
+    "spmv_mlp_save": (S, [P, C.c_char_p]),
+    "spmv_mlp_load": (S, [C.c_char_p, C.POINTER(P)]),
+    "spmv_select": (S, [C.POINTER(Handle), I, P, I, I, I, I, I, P, P, P, C.POINTER(Variant), C.POINTER(C.c_int)]),
+    "spmv_set_selector": (S, [C.POINTER(Handle), P]),
 }
+
+NUM_FEATURES = 32
+SELECT_HEURISTIC, SELECT_LEARNED, SELECT_AUTOTUNE, SELECT_LEARNED_TOPK = range(4)
 
 _lib = None
 

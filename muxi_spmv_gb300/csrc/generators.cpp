@@ -418,6 +418,29 @@ spmv_status_t vec(long long n, unsigned long long seed, double lo, double hi, T*
 
 }  // namespace
 
+namespace mxs {
+// Inverse-CDF table of the row-length law of `p` (POISSON_UNIFORM, POWERLAW,
+// ZIPF_UNIFORM, BANDED, BLOCKDIAG): lengths are first + index of the first
+// cdf entry above a uniform draw.  Returns false for laws without a table.
+bool gen_length_table(const spmv_gen_params_t& p, std::vector<double>& cdf, int& first) {
+    Gen g(p);
+    if (!g.hasTable) return false;
+    cdf = g.lenTable.cdf;
+    first = g.lenTable.first;
+    return true;
+}
+// Mean of the truncated Zipf(s) law on [1, M].
+double zipf_mean(double s, int M) {
+    double num = 0.0, den = 0.0;
+    for (int k = 1; k <= M; ++k) {
+        const double w = det_exp(-s * det_log((double)k));
+        num += k * w;
+        den += w;
+    }
+    return num / den;
+}
+}  // namespace mxs
+
 extern "C" {
 
 spmv_status_t spmv_gen_row_ptr(const spmv_gen_params_t* p, int* rowPtr, long long* nnz) {

@@ -30,6 +30,7 @@ inline unsigned grid_for(long long work, int per_block) {
 // Internal state hanging off spmv_handle_t::internal.
 struct HandleState {
     int device = 0;
+    spmv_mlp_t selector = nullptr;  // borrowed; AUTO plans consult it when set
 };
 
 // Per-device properties cached on first use (SM count, L2 size, smem).

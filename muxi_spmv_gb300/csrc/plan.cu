@@ -133,6 +133,18 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
     p->values = values;
     p->device = h->deviceId;
     p->variant = resolve(variant, R, N);
+    const HandleState* hs = static_cast<const HandleState*>(h->internal);
+    if ((!variant || variant->kernel == SPMV_KERNEL_AUTO) && hs && hs->selector && R > 0 && N > 0) {
+        std::vector<int> order;
+        spmv_status_t sst = learned_rank(hs->selector, type, R, C, N, rowPtr, colIdx, h->stream, order);
+        if (sst != SPMV_SUCCESS) {
+            delete p;
+            return sst;
+        }
+        std::vector<spmv_variant_t> space(spmv_variant_space(nullptr, 0));
+        spmv_variant_space(space.data(), (int)space.size());
+        p->variant = resolve(&space[order[0]], R, N);
+    }
     const size_t vs = type == SPMV_TYPE_FLOAT ? 4 : 8;
 
     spmv_status_t st = SPMV_SUCCESS;
