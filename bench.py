@@ -266,7 +266,11 @@ def gpu_arm(args):
     value = ws * nbytes / (step_ms * 1e-3) / 1e9
     e2e_val = ws * nbytes / (e2e_ms * 1e-3) / 1e9
     pv = plan.variant.as_dict()
-    launches_per_step = 2 if pv["kernel"] == mx.KERNEL_MERGE else 1
+    kern_names = {mx.KERNEL_MERGE: "merge_vec_kernel", mx.KERNEL_CSR5: "csr5_tile_kernel",
+                  mx.KERNEL_BAND: "band_block_kernel", mx.KERNEL_ELL: "ell_kernel",
+                  mx.KERNEL_SCALAR: "csr_rows_kernel", mx.KERNEL_VECTOR: "csr_rows_kernel"}
+    # merge-path, CSR5 and band plans launch the tile kernel and a carry fix-up
+    launches_per_step = 2 if pv["kernel"] in (mx.KERNEL_MERGE, mx.KERNEL_CSR5, mx.KERNEL_BAND) else 1
 
     traffic = None
     tf = ROOT / "profiles" / f"traffic_{args.workload}_{args.dtype}.json"
@@ -285,7 +289,7 @@ def gpu_arm(args):
                        "gflops": round(2 * A.nnz / (step_ms * 1e-3) / 1e9, 2), "generate_s": round(gen_s, 2)},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                         "kernel": "merge_tile_kernel" if launches_per_step == 2 else "csr_rows_kernel",
+                         "kernel": kern_names.get(pv["kernel"], str(pv["kernel"])),
                          "kernel_ms": round(kern_ms, 5), "traffic": traffic},
             "e2e": {"value": round(e2e_val, 3), "unit": UNIT, "h2d_bytes_per_step": int(A.numCols * vs),
                     "d2h_bytes_per_step": int(A.numRows * vs), "ms_per_step": round(e2e_ms, 5),
@@ -317,6 +321,180 @@ def gpu_arm(args):
         dist.destroy_process_group()
 
 
+def batched_arm(args):
+    """Uneven batch: 1,024 CSR matrices (rows log-uniform [1,024, 262,144],
+    mean row length U[2,64], Poisson or Zipf(2.0) lengths), k right-hand
+    sides.  One JSON line per k: batches/s of the persistent launch replayed
+    from a CUDA graph, against the per-matrix loop (plain launches and graph).
+    X blocks of all matrices live in one device buffer (16-byte aligned
+    slices), so the e2e number moves them with one pinned copy each way."""
+    import ctypes as C
+
+    import torch
+
+    import muxi_spmv_gb300 as mx
+    from muxi_spmv_gb300 import batch as B
+    from muxi_spmv_gb300 import selector as S
+    import oracle
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    h = mx.spmv_create_handle()
+    h.set_stream(stream)
+    t0 = time.time()
+    specs = B.uneven_specs(args.batch_count, seed=rank)
+    mats = [S.gen_device(s.spec) for s in specs]
+    torch.cuda.synchronize()
+    gen_s = time.time() - t0
+    distinct = [mx.count_distinct_columns(A, stream) for A in mats]
+    sumN = sum(A.nnz for A in mats)
+    sumR = sum(A.numRows for A in mats)
+    sumC = sum(A.numCols for A in mats)
+    peak, peak_kind = peaks()
+    L = mx.lib()
+
+    def aligned_slices(sizes):
+        offs, o = [], 0
+        for n in sizes:
+            offs.append(o)
+            o += (n + 3) // 4 * 4
+        return offs, max(o, 4)
+
+    for k in [int(z) for z in args.k.split(",")]:
+        xo, xn = aligned_slices([A.numCols * k for A in mats])
+        yo, yn = aligned_slices([A.numRows * k for A in mats])
+        Xd = torch.empty(xn, dtype=torch.float32, device=dev)
+        Yd = torch.empty(yn, dtype=torch.float32, device=dev)
+        mx.check(L.spmv_gen_device_vector_f32(xn, 1000 + k, -1.0, 1.0, Xd.data_ptr(), None), "gen x")
+        xs = [Xd[o:o + A.numCols * k] for o, A in zip(xo, mats)]
+        ys = [Yd[o:o + max(A.numRows * k, 1)] for o, A in zip(yo, mats)]
+        plan = B.BatchPlan(h, mats, k)
+        plan.set_vectors(xs, ys)
+        info = plan.info()
+        plan.exec(1.0, 0.0, B.BATCH_PERSISTENT_GRAPH)
+        stream.synchronize()
+
+        # parity on sampled matrices (all k columns) against the FP64 oracle
+        worst, checked = 0.0, 0
+        for i in np.linspace(0, len(mats) - 1, args.parity_samples).astype(int):
+            A = mats[i]
+            rp = A.d_rowPtr.cpu().numpy()
+            ci = A.d_colIdx[:A.nnz].cpu().numpy()
+            v = A.d_values[:A.nnz].cpu().numpy()
+            X = xs[i].cpu().numpy().reshape(A.numCols, k)
+            Y = ys[i][:A.numRows * k].cpu().numpy().reshape(A.numRows, k)
+            for j in range(k):
+                yr, absum = oracle.spmv_ref(rp, ci, v, np.ascontiguousarray(X[:, j]))
+                worst = max(worst, float(oracle.row_errors(Y[:, j], yr, absum, 1e-5).max()))
+                checked += A.numRows
+        if worst > 1.0:
+            print(f"PARITY FAILURE k={k}: {worst}", file=sys.stderr)
+
+        nbytes = sum(A.nnz * 8 + (A.numRows + 1) * 4 + k * A.numRows * 4 + k * d * 4 for A, d in zip(mats, distinct))
+        times = {}
+        clocks = ClockSampler(local)
+        clocks.start()
+        time.sleep(0.3)
+        for name, mode, steps in (("persistent_graph", B.BATCH_PERSISTENT_GRAPH, args.steps),
+                                  ("persistent", B.BATCH_PERSISTENT, args.steps),
+                                  ("loop", B.BATCH_LOOP, max(3, args.steps // 4)),
+                                  ("loop_graph", B.BATCH_LOOP_GRAPH, max(3, args.steps // 4))):
+            for _ in range(args.warmup):
+                plan.exec(1.0, 0.0, mode)
+            stream.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                plan.exec(1.0, 0.0, mode)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            times[name] = e0.elapsed_time(e1) / steps
+
+        # end to end: pinned host X in, Y out, persistent graph in between
+        Xh = torch.empty(xn, dtype=torch.float32).pin_memory()
+        Yh = torch.empty(yn, dtype=torch.float32).pin_memory()
+        Xh.copy_(Xd.cpu())
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                Xd.copy_(Xh, non_blocking=True)
+                plan.exec(1.0, 0.0, B.BATCH_PERSISTENT_GRAPH)
+                Yh.copy_(Yd, non_blocking=True)
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            for _ in range(args.steps):
+                Xd.copy_(Xh, non_blocking=True)
+                plan.exec(1.0, 0.0, B.BATCH_PERSISTENT_GRAPH)
+                Yh.copy_(Yd, non_blocking=True)
+            f1.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e_ms = f0.elapsed_time(f1) / args.steps
+        clocks.stop()
+        if ws > 1:
+            t = torch.tensor([times["persistent_graph"], e2e_ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            times["persistent_graph"], e2e_ms = t.tolist()
+
+        ms = times["persistent_graph"]
+        achieved = nbytes / (ms * 1e-3) / 1e9
+        line = {"metric": "batched_spmm_batches_per_s", "value": round(ws * 1e3 / ms, 3), "unit": "batch/s",
+                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 5),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded device generators)",
+                "config": {"workload": f"uneven{args.batch_count}", "k": k, "matrices": len(mats), "rows": sumR,
+                           "cols": sumC, "nnz": sumN, "algorithmic_bytes": int(nbytes), "tiles": info["tiles"],
+                           "warps": info["warps"], "l2": "inputs larger than L2 (no flush)",
+                           "parallelism": f"replicas{ws}", "generate_s": round(gen_s, 2),
+                           "gflops": round(2 * sumN * k / (ms * 1e-3) / 1e9, 2),
+                           "ms": {n: round(t, 4) for n, t in times.items()},
+                           "speedup_vs_loop": round(times["loop"] / ms, 3),
+                           "speedup_vs_loop_graph": round(times["loop_graph"] / ms, 3)},
+                "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                             "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                             "kernel": f"batch_tile_kernel<{k}> + batch_fixup_kernel<{k}> (graph)",
+                             "traffic": None},
+                "e2e": {"value": round(ws * 1e3 / e2e_ms, 3), "unit": "batch/s", "h2d_bytes_per_step": int(xn * 4),
+                        "d2h_bytes_per_step": int(yn * 4), "ms_per_step": round(e2e_ms, 5),
+                        "call": "spmv_batch_exec_f32 (persistent graph) with pinned X/Y copies"},
+                "gpu_launches": 2 * args.steps,
+                "clocks": clocks.summary(),
+                "parity": {"matrices_checked": int(args.parity_samples), "rows_checked": checked,
+                           "max_err_over_bound": worst}}
+        if rank == 0 and not args.no_cpu_baseline:
+            # bounded sample: the reference CPU loop over 64 matrices, k passes each
+            threads = os.cpu_count() or 1
+            idx = np.linspace(0, len(mats) - 1, 64).astype(int)
+            host = []
+            for i in idx:
+                A = mats[i]
+                host.append((A.d_rowPtr.cpu().numpy(), A.d_colIdx[:A.nnz].cpu().numpy(),
+                             A.d_values[:A.nnz].cpu().numpy(), xs[i].cpu().numpy().reshape(A.numCols, k)))
+            nn = sum(int(rp[-1]) for rp, *_ in host)
+            t = time.perf_counter()
+            for rp, ci, v, X in host:
+                for j in range(k):
+                    oracle.cpu_spmv(rp, ci, v, np.ascontiguousarray(X[:, j]), threads=threads)
+            cpu_s = (time.perf_counter() - t) * sumN / max(nn, 1)
+            line["cpu_baseline"] = {"value": round(1.0 / cpu_s, 4), "unit": "batch/s", "cores": threads,
+                                    "kind": "port",
+                                    "sample": f"64 of {len(mats)} matrices ({nn} nonzeros), reference CPU loop per "
+                                              f"column, scaled to the batch's {sumN} nonzeros"}
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        plan.destroy()
+        del Xd, Yd, xs, ys, Xh, Yh
+        torch.cuda.empty_cache()
+    h.destroy()
+    if ws > 1:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -328,11 +506,20 @@ def main():
     ap.add_argument("--variant", default="", help="kernel,block,tpr,ipt,vec (spmv_variant_t)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scale-rows", type=int, default=0, help="same law on this many rows (profiling cases)")
+    ap.add_argument("--k", default="1,2,4,8,16", help="right-hand sides (uneven batch workload)")
+    ap.add_argument("--batch-count", type=int, default=1024, help="matrices (uneven batch workload)")
+    ap.add_argument("--parity-samples", type=int, default=8, help="matrices checked (uneven batch workload)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    batched = args.workload.startswith("uneven")
     if args.impl == "reference":
-        cpu_reference_arm(args)
+        if batched:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched multi-matrix path"}))
+        else:
+            cpu_reference_arm(args)
+    elif batched:
+        batched_arm(args)
     else:
         gpu_arm(args)
 

@@ -422,7 +422,9 @@ typedef enum {
                                       clamped to the block; columns uniform
                                       inside the block                        */
     SPMV_GEN_ZIPF_UNIFORM = 6,     /* Zipf(p0) lengths truncated to [1,p1],
-                                      columns uniform without replacement     */
+                                      plus p2 on every row (0 = none), capped
+                                      at numCols; columns uniform without
+                                      replacement                             */
     SPMV_GEN_DIAGONAL = 7          /* identity pattern, values 1              */
 } spmv_gen_kind_t;
 
@@ -543,6 +545,44 @@ SPMV_API spmv_status_t spmv_select(spmv_handle_t* handle, spmv_select_mode_t mod
  * created with SPMV_KERNEL_AUTO then take the learned pick.  The handle
  * borrows the model; it must outlive the handle's use of it. */
 SPMV_API spmv_status_t spmv_set_selector(spmv_handle_t* handle, spmv_mlp_t model);
+
+/* ------------------------------------------------------------------ */
+/* Batched SpMV / SpMM over many independent FP32 CSR matrices:          */
+/* Y_i = alpha*A_i*X_i + beta*Y_i, X_i numCols_i x k and Y_i numRows_i x k */
+/* row-major on the device, k in {1, 2, 4, 8, 16}.  No counterpart in    */
+/* the reference (its multi-stream test splits one matrix,               */
+/* tests/test_multi_stream.cu:121-236).  The batch borrows the matrices; */
+/* colIdx and values must be 16-byte aligned, X_i and Y_i aligned to     */
+/* min(k,4)*4 bytes.  Results are deterministic (no atomics).            */
+/* ------------------------------------------------------------------ */
+typedef struct spmv_batch_s* spmv_batch_t;
+typedef struct {
+    int numRows;
+    int numCols;
+    int nnz;
+    const int* rowPtr;
+    const int* colIdx;
+    const float* values;
+} spmv_batch_matrix_t;
+
+typedef enum {
+    SPMV_BATCH_PERSISTENT = 0,        /* one launch over all matrices (+ fix-up)   */
+    SPMV_BATCH_PERSISTENT_GRAPH = 1,  /* the same, replayed from a CUDA graph       */
+    SPMV_BATCH_LOOP = 2,              /* one launch per matrix (baseline)           */
+    SPMV_BATCH_LOOP_GRAPH = 3         /* the per-matrix loop replayed from a graph  */
+} spmv_batch_mode_t;
+
+/* `mats` is a host array of `count` descriptors (device pointers).  Builds
+ * the tile table (synchronises the handle's stream). */
+SPMV_API spmv_status_t spmv_batch_create(spmv_handle_t* handle, int count, const spmv_batch_matrix_t* mats, int k,
+                                         spmv_batch_t* batch);
+SPMV_API spmv_status_t spmv_batch_destroy(spmv_batch_t batch);
+/* x, y: host arrays of `count` device pointers.  Binds the vectors used by
+ * every later execution (graphs stay valid; synchronous copy). */
+SPMV_API spmv_status_t spmv_batch_set_vectors_f32(spmv_batch_t batch, const float* const* x, float* const* y);
+SPMV_API spmv_status_t spmv_batch_exec_f32(spmv_handle_t* handle, spmv_batch_t batch, float alpha, float beta,
+                                           spmv_batch_mode_t mode);
+SPMV_API spmv_status_t spmv_batch_info(spmv_batch_t batch, long long* tiles, int* warps, long long* nnzTotal);
 
 #ifdef __cplusplus
 }

@@ -66,6 +66,12 @@ class GenParams(C.Structure):
                 ("threads", C.c_int)]
 
 
+class BatchMatrix(C.Structure):
+    """spmv_batch_matrix_t."""
+    _fields_ = [("numRows", C.c_int), ("numCols", C.c_int), ("nnz", C.c_int), ("rowPtr", C.c_void_p),
+                ("colIdx", C.c_void_p), ("values", C.c_void_p)]
+
+
 P = C.c_void_p
 I = C.c_int
 F = C.c_float
@@ -146,7 +152,14 @@ SIGNATURES = {
     "spmv_mlp_load": (S, [C.c_char_p, C.POINTER(P)]),
     "spmv_select": (S, [C.POINTER(Handle), I, P, I, I, I, I, I, P, P, P, C.POINTER(Variant), C.POINTER(C.c_int)]),
     "spmv_set_selector": (S, [C.POINTER(Handle), P]),
+    "spmv_batch_create": (S, [C.POINTER(Handle), I, C.POINTER(BatchMatrix), I, C.POINTER(P)]),
+    "spmv_batch_destroy": (S, [P]),
+    "spmv_batch_set_vectors_f32": (S, [P, C.POINTER(P), C.POINTER(P)]),
+    "spmv_batch_exec_f32": (S, [C.POINTER(Handle), P, F, F, I]),
+    "spmv_batch_info": (S, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
 }
+
+BATCH_PERSISTENT, BATCH_PERSISTENT_GRAPH, BATCH_LOOP, BATCH_LOOP_GRAPH = range(4)
 
 NUM_FEATURES = 32
 SELECT_HEURISTIC, SELECT_LEARNED, SELECT_AUTOTUNE, SELECT_LEARNED_TOPK = range(4)

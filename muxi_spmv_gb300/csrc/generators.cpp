@@ -198,8 +198,13 @@ struct Gen {
                 break;
             }
             case SPMV_GEN_POWERLAW:
-            case SPMV_GEN_ZIPF_UNIFORM:
                 lenTable = zipf_table(p.p0, std::max(1, (int)p.p1));
+                hasTable = true;
+                break;
+            case SPMV_GEN_ZIPF_UNIFORM:
+                // p2 >= 1 shifts every length up by p2 (mean beyond Zipf's own).
+                lenTable = zipf_table(p.p0, std::max(1, (int)p.p1));
+                lenTable.first += std::max(0, (int)p.p2);
                 hasTable = true;
                 break;
             case SPMV_GEN_BANDED:

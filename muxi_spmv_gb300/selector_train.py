@@ -1,0 +1,301 @@
+"""Builds the learned kernel selector: corpus, training, evaluation.
+
+    python -m muxi_spmv_gb300.selector_train corpus --out DIR [--count 4000]
+    python -m muxi_spmv_gb300.selector_train train --corpus DIR --model OUT.mxsmlp
+    python -m muxi_spmv_gb300.selector_train evaluate --corpus DIR --model OUT.mxsmlp
+
+corpus: seeded matrices generated on the GPU, one law per seed -- Poisson row
+lengths, Zipf lengths (s in [1.3, 2.5]), banded (width 3..1025) and
+block-diagonal (8..256 blocks) -- with rows log-uniform in [1e4, 1e7] and mean
+row length log-uniform in [2, 128], FP32 N(0,1) values.  Each matrix gets its
+32 features (spmv_matrix_features) and the exhaustive autotuner's time for
+every variant of the space plus the reference heuristic's pick.  Records are
+written in chunks, so an interrupted run resumes where it stopped.
+
+train: targets are log(time / best time) per variant, masked where a variant
+does not apply; seeds with seed % 5 == 0 are held out (80/20 split by seed).
+The network (32 -> 128 -> 128 -> variants) is trained on the GPU by the
+library's own kernels (spmv_mlp_train_step).
+
+evaluate: regret = time of the pick / best time - 1 on the held-out seeds,
+for the learned selector, the reference heuristic (src/spmv/csr/spmv_csr.cu:
+115-153) and the fixed default (CSR5, 256-nonzero tiles); selection cost =
+wall time of spmv_select(LEARNED) against the autotuner's wall time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+from . import api, selector
+from .api import GenSpec, GEN_BANDED, GEN_BLOCKDIAG, GEN_POISSON_UNIFORM, GEN_ZIPF_UNIFORM, Variant
+
+LAWS = ("poisson", "zipf", "banded", "blockdiag")
+HEURISTIC_COL = -1  # last column of the label matrix: the heuristic's variant
+DEFAULT_VARIANT = Variant(api.KERNEL_CSR5, 256, 0, 8, 1)
+
+
+def _zipf_clip_for_mean(s: float, target: float, cap: int) -> int:
+    """Largest truncation K <= cap whose Zipf(s) mean is <= target (at least 1)."""
+    K = np.arange(1, cap + 1, dtype=np.float64)
+    w = K ** (-s)
+    mean = np.cumsum(w * K) / np.cumsum(w)
+    k = int(np.searchsorted(mean, target, side="right"))
+    return max(1, min(cap, k))
+
+
+def spec_for_seed(seed: int, max_rows: int = 10_000_000, max_nnz: int = 600_000_000):
+    """The corpus matrix of `seed`: (GenSpec, law name, target mean row length)."""
+    rng = np.random.default_rng(np.random.SeedSequence([0x5E1EC7, seed]))
+    law = LAWS[seed % 4] if seed >= 0 else LAWS[0]
+    lo = math.log10(1e4)
+    R = int(round(10 ** rng.uniform(lo, math.log10(max_rows))))
+    m = float(10 ** rng.uniform(math.log10(2.0), math.log10(128.0)))
+    if R * m > max_nnz:
+        R = max(10_000, int(max_nnz / m))
+    C = R
+    gseed = 1_000_003 * seed + 17
+    if law == "poisson":
+        spec = GenSpec(GEN_POISSON_UNIFORM, R, C, m, 0.0, float(min(C, int(4 * m + 64))), 0.0, gseed)
+    elif law == "zipf":
+        s = float(rng.uniform(1.3, 2.5))
+        clip = _zipf_clip_for_mean(s, m, min(C, 1 << 20))
+        spec = GenSpec(GEN_ZIPF_UNIFORM, R, C, s, float(clip), 0.0, 0.0, gseed)
+    elif law == "banded":
+        w = int(round(10 ** rng.uniform(math.log10(3), math.log10(1025))))
+        w = max(3, min(w, C))
+        spec = GenSpec(GEN_BANDED, R, C, min(m, float(w)), float(w), 0.0, 0.0, gseed)
+    else:
+        nb = int(rng.integers(8, 257))
+        spec = GenSpec(GEN_BLOCKDIAG, R, C, float(nb), m, 0.0, 0.0, gseed)
+    return spec, law, m
+
+
+def heuristic_variant(R: int, N: int) -> Variant:
+    """The reference's dispatch rule (src/spmv/csr/spmv_csr.cu:115-153)."""
+    avg = N // max(R, 1)
+    if avg < 32:
+        return Variant(api.KERNEL_SCALAR, 256, 1, 0, 1)
+    return Variant(api.KERNEL_VECTOR, 256, 32, 0, 1)
+
+
+def label_one(handle, seed: int, max_rows: int, max_nnz: int):
+    """Generates, featurises and autotunes one corpus matrix."""
+    import torch
+    spec, law, m = spec_for_seed(seed, max_rows, max_nnz)
+    A = selector.gen_device(spec)
+    torch.cuda.synchronize()
+    feats = selector.matrix_features(A).cpu().numpy()
+    space = selector.variant_space()
+    cands = space + [heuristic_variant(A.numRows, A.nnz)]
+    t0 = time.perf_counter()
+    ms, _ = selector.autotune(handle, A, cands, repeats=0)
+    torch.cuda.synchronize()
+    tune_s = time.perf_counter() - t0
+    meta = np.array([seed, LAWS.index(law), A.numRows, A.numCols, A.nnz, m, tune_s], np.float64)
+    del A
+    return feats, ms, meta
+
+
+def cmd_corpus(a):
+    import torch
+    out = Path(a.out)
+    out.mkdir(parents=True, exist_ok=True)
+    handle = api.SpmvHandle()
+    torch.cuda.init()
+    t_start = time.perf_counter()
+    for c0 in range(a.start, a.start + a.count, a.chunk):
+        path = out / f"corpus_{c0:06d}.npz"
+        if path.exists():
+            continue
+        F, L, Mt = [], [], []
+        for seed in range(c0, min(c0 + a.chunk, a.start + a.count)):
+            f, ms, meta = label_one(handle, seed, a.max_rows, a.max_nnz)
+            F.append(f)
+            L.append(ms)
+            Mt.append(meta)
+            torch.cuda.empty_cache()
+        tmp = out / f".corpus_{c0:06d}.tmp.npz"
+        np.savez(tmp, features=np.stack(F), ms=np.stack(L), meta=np.stack(Mt))
+        tmp.rename(path)
+        el = time.perf_counter() - t_start
+        print(f"chunk {c0}: {len(F)} matrices, {el:.0f}s elapsed", flush=True)
+        if a.time_limit and el > a.time_limit:
+            print("time limit reached; rerun to resume", flush=True)
+            break
+
+
+def load_corpus(d) -> dict:
+    files = sorted(Path(d).glob("corpus_*.npz"))
+    if not files:
+        raise FileNotFoundError(f"no corpus chunks in {d}")
+    parts = [np.load(f) for f in files]
+    return {k: np.concatenate([p[k] for p in parts]) for k in ("features", "ms", "meta")}
+
+
+def targets(ms_space: np.ndarray, clip: float = math.log(20.0)):
+    """log slowdown vs the best applicable variant, and the applicability mask."""
+    M = (ms_space > 0).astype(np.float32)
+    best = np.where(M > 0, ms_space, np.inf).min(1, keepdims=True)
+    T = np.where(M > 0, np.log(np.maximum(ms_space, 1e-9) / best), 0.0)
+    return np.minimum(T, clip).astype(np.float32), M
+
+
+def split(meta: np.ndarray):
+    test = (meta[:, 0].astype(np.int64) % 5) == 0
+    return ~test, test
+
+
+def regrets(pred_or_pick, ms_space: np.ndarray, ms_pick=None):
+    """Per-matrix regret of a pick: picks index the space, or ms_pick gives times."""
+    valid = ms_space > 0
+    best = np.where(valid, ms_space, np.inf).min(1)
+    if ms_pick is None:
+        pick = pred_or_pick
+        t = ms_space[np.arange(len(pick)), pick]
+    else:
+        t = ms_pick
+    return t / best - 1.0
+
+
+def learned_picks(pred: np.ndarray, ms_space: np.ndarray):
+    return np.where(ms_space > 0, pred, np.inf).argmin(1)
+
+
+def cmd_train(a):
+    import torch
+    data = load_corpus(a.corpus)
+    ms = data["ms"][:, :HEURISTIC_COL]
+    tr, te = split(data["meta"])
+    X = data["features"].astype(np.float32)
+    T, M = targets(ms)
+    mean = X[tr].mean(0)
+    std = X[tr].std(0)
+    nvar = ms.shape[1]
+    model = selector.MLP(X.shape[1], a.hidden, a.hidden, nvar, seed=a.seed)
+    model.set_normalization(mean, np.where(std > 1e-6, std, 1.0))
+    dev = torch.device("cuda")
+    Xtr, Ttr, Mtr = (torch.from_numpy(v[tr]).to(dev).contiguous() for v in (X, T, M))
+    n = Xtr.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(a.seed)
+    t0 = time.perf_counter()
+    step = 0
+    for ep in range(a.epochs):
+        perm = torch.randperm(n, generator=g).to(dev)
+        lr = a.lr * 0.5 * (1 + math.cos(math.pi * ep / a.epochs))
+        for i in range(0, n, a.batch):
+            idx = perm[i:i + a.batch]
+            model.train_step(Xtr[idx].contiguous(), Ttr[idx].contiguous(), Mtr[idx].contiguous(), lr)
+            step += 1
+        if (ep + 1) % max(1, a.epochs // 10) == 0:
+            loss, _ = model.gradients(Xtr, Ttr, Mtr)
+            print(f"epoch {ep + 1}: train loss {loss:.4f}", flush=True)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    model.save(a.model)
+    rep = evaluate(model, data)
+    rep["train_seconds"] = train_s
+    rep["train_steps"] = step
+    print(json.dumps(rep, indent=1))
+    if a.report:
+        Path(a.report).write_text(json.dumps(rep, indent=1) + "\n")
+
+
+def evaluate(model, data, split_name: str = "test") -> dict:
+    import torch
+    ms_all = data["ms"]
+    ms = ms_all[:, :HEURISTIC_COL]
+    tr, te = split(data["meta"])
+    sel = te if split_name == "test" else tr
+    X = torch.from_numpy(data["features"][sel].astype(np.float32)).cuda()
+    pred = model.forward(X).cpu().numpy()
+    picks = learned_picks(pred, ms[sel])
+    r_learn = regrets(picks, ms[sel])
+    r_heur = regrets(None, ms[sel], ms_pick=ms_all[sel, HEURISTIC_COL])
+    space = selector.variant_space()
+    di = next(i for i, v in enumerate(space) if (v.kernel, v.blockSize, v.itemsPerThread) ==
+              (DEFAULT_VARIANT.kernel, DEFAULT_VARIANT.blockSize, DEFAULT_VARIANT.itemsPerThread))
+    r_def = regrets(np.full(sel.sum(), di), ms[sel])
+    best = np.where(ms[sel] > 0, ms[sel], np.inf).argmin(1)
+
+    def stats(r):
+        return {"mean": float(np.mean(r)), "p95": float(np.percentile(r, 95)), "max": float(np.max(r))}
+
+    return {"split": split_name, "matrices": int(sel.sum()), "learned_regret": stats(r_learn),
+            "heuristic_regret": stats(r_heur), "default_csr5_regret": stats(r_def),
+            "top1_accuracy": float(np.mean(picks == best)),
+            "autotune_seconds_median": float(np.median(data["meta"][sel, 6]))}
+
+
+def selection_cost(model, count: int = 8, max_rows: int = 2_000_000) -> dict:
+    """Wall time of spmv_select(LEARNED) vs spmv_autotune on a few matrices."""
+    import torch
+    h = api.SpmvHandle()
+    t_sel, t_tune = [], []
+    for seed in range(5, 5 + 5 * count, 5):
+        spec, _, _ = spec_for_seed(seed, max_rows)
+        A = selector.gen_device(spec)
+        torch.cuda.synchronize()
+        selector.select(h, A, selector.SELECT_LEARNED, model)  # warm
+        t0 = time.perf_counter()
+        for _ in range(10):
+            selector.select(h, A, selector.SELECT_LEARNED, model)
+        torch.cuda.synchronize()
+        t_sel.append((time.perf_counter() - t0) / 10)
+        t0 = time.perf_counter()
+        selector.autotune(h, A, None, repeats=0)
+        torch.cuda.synchronize()
+        t_tune.append(time.perf_counter() - t0)
+        del A
+    s, t = float(np.median(t_sel)), float(np.median(t_tune))
+    return {"select_ms_median": s * 1e3, "autotune_ms_median": t * 1e3, "cost_ratio": t / s}
+
+
+def cmd_evaluate(a):
+    data = load_corpus(a.corpus)
+    model = selector.MLP.load(a.model)
+    rep = {"test": evaluate(model, data, "test"), "train": evaluate(model, data, "train")}
+    if a.cost:
+        rep["selection_cost"] = selection_cost(model)
+    print(json.dumps(rep, indent=1))
+    if a.report:
+        Path(a.report).write_text(json.dumps(rep, indent=1) + "\n")
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser(prog="python -m muxi_spmv_gb300.selector_train")
+    sub = p.add_subparsers(dest="cmd", required=True)
+    c = sub.add_parser("corpus")
+    c.add_argument("--out", required=True)
+    c.add_argument("--start", type=int, default=0)
+    c.add_argument("--count", type=int, default=4000)
+    c.add_argument("--chunk", type=int, default=100)
+    c.add_argument("--max-rows", type=int, default=10_000_000)
+    c.add_argument("--max-nnz", type=int, default=600_000_000)
+    c.add_argument("--time-limit", type=float, default=0.0, help="seconds; stop after the chunk that passes it")
+    t = sub.add_parser("train")
+    t.add_argument("--corpus", required=True)
+    t.add_argument("--model", required=True)
+    t.add_argument("--hidden", type=int, default=128)
+    t.add_argument("--epochs", type=int, default=400)
+    t.add_argument("--batch", type=int, default=128)
+    t.add_argument("--lr", type=float, default=2e-3)
+    t.add_argument("--seed", type=int, default=0)
+    t.add_argument("--report")
+    e = sub.add_parser("evaluate")
+    e.add_argument("--corpus", required=True)
+    e.add_argument("--model", required=True)
+    e.add_argument("--cost", action="store_true")
+    e.add_argument("--report")
+    a = p.parse_args(argv)
+    {"corpus": cmd_corpus, "train": cmd_train, "evaluate": cmd_evaluate}[a.cmd](a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())
