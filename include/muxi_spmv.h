@@ -572,10 +572,23 @@ typedef enum {
     SPMV_BATCH_LOOP_GRAPH = 3         /* the per-matrix loop replayed from a graph  */
 } spmv_batch_mode_t;
 
+/* Launch shape of a batch (0 in a field = its default): nonzeros per slot
+ * of 8 lanes' work (8, or 16 for k <= 2; default 8), resident blocks per SM
+ * the kernel is compiled for (2 or 3; default 2), and nonzeros per work
+ * chunk handed to a warp (a multiple of the tile; default 2048). */
+typedef struct {
+    int nnzPerSlot;
+    int blocksPerSM;
+    int chunkNnz;
+} spmv_batch_variant_t;
+
 /* `mats` is a host array of `count` descriptors (device pointers).  Builds
  * the tile table (synchronises the handle's stream). */
 SPMV_API spmv_status_t spmv_batch_create(spmv_handle_t* handle, int count, const spmv_batch_matrix_t* mats, int k,
                                          spmv_batch_t* batch);
+SPMV_API spmv_status_t spmv_batch_create_ex(spmv_handle_t* handle, int count, const spmv_batch_matrix_t* mats,
+                                            int k, const spmv_batch_variant_t* variant, spmv_batch_t* batch);
+SPMV_API spmv_status_t spmv_batch_get_variant(spmv_batch_t batch, spmv_batch_variant_t* variant);
 SPMV_API spmv_status_t spmv_batch_destroy(spmv_batch_t batch);
 /* x, y: host arrays of `count` device pointers.  Binds the vectors used by
  * every later execution (graphs stay valid; synchronous copy). */

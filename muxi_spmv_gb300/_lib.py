@@ -72,6 +72,14 @@ class BatchMatrix(C.Structure):
                 ("colIdx", C.c_void_p), ("values", C.c_void_p)]
 
 
+class BatchVariant(C.Structure):
+    """spmv_batch_variant_t."""
+    _fields_ = [("nnzPerSlot", C.c_int), ("blocksPerSM", C.c_int), ("chunkNnz", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 P = C.c_void_p
 I = C.c_int
 F = C.c_float
@@ -153,6 +161,9 @@ SIGNATURES = {
     "spmv_select": (S, [C.POINTER(Handle), I, P, I, I, I, I, I, P, P, P, C.POINTER(Variant), C.POINTER(C.c_int)]),
     "spmv_set_selector": (S, [C.POINTER(Handle), P]),
     "spmv_batch_create": (S, [C.POINTER(Handle), I, C.POINTER(BatchMatrix), I, C.POINTER(P)]),
+    "spmv_batch_create_ex": (S, [C.POINTER(Handle), I, C.POINTER(BatchMatrix), I, C.POINTER(BatchVariant),
+                                 C.POINTER(P)]),
+    "spmv_batch_get_variant": (S, [P, C.POINTER(BatchVariant)]),
     "spmv_batch_destroy": (S, [P]),
     "spmv_batch_set_vectors_f32": (S, [P, C.POINTER(P), C.POINTER(P)]),
     "spmv_batch_exec_f32": (S, [C.POINTER(Handle), P, F, F, I]),

@@ -13,7 +13,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from ._lib import (BATCH_LOOP, BATCH_LOOP_GRAPH, BATCH_PERSISTENT, BATCH_PERSISTENT_GRAPH,  # noqa: F401
-                   BatchMatrix, check, lib)
+                   BatchMatrix, BatchVariant, check, lib)
 from .api import GEN_POISSON_UNIFORM, GEN_ZIPF_UNIFORM, GenSpec, SpmvHandle, _ptr, _torch
 
 
@@ -21,7 +21,7 @@ class BatchPlan:
     """A batch of device CSR matrices (CSRMatrix on the device or DeviceCSR)
     bound to k right-hand sides."""
 
-    def __init__(self, handle: SpmvHandle, mats, k: int):
+    def __init__(self, handle: SpmvHandle, mats, k: int, variant: dict | None = None):
         self.handle = handle
         self.mats = list(mats)  # keeps the borrowed arrays alive
         self.k = k
@@ -29,7 +29,9 @@ class BatchPlan:
         for i, A in enumerate(self.mats):
             arr[i] = BatchMatrix(A.numRows, A.numCols, A.nnz, _ptr(A.d_rowPtr), _ptr(A.d_colIdx), _ptr(A.d_values))
         b = C.c_void_p()
-        check(lib().spmv_batch_create(handle.raw, len(self.mats), arr, k, C.byref(b)), "spmv_batch_create")
+        v = BatchVariant(**(variant or {}))
+        check(lib().spmv_batch_create_ex(handle.raw, len(self.mats), arr, k, C.byref(v), C.byref(b)),
+              "spmv_batch_create_ex")
         self._b = b
         self.xs = self.ys = None
 
@@ -43,6 +45,12 @@ class BatchPlan:
 
     def exec(self, alpha: float = 1.0, beta: float = 0.0, mode: int = BATCH_PERSISTENT_GRAPH):
         check(lib().spmv_batch_exec_f32(self.handle.raw, self._b, alpha, beta, mode), "spmv_batch_exec_f32")
+
+    @property
+    def variant(self) -> dict:
+        v = BatchVariant()
+        check(lib().spmv_batch_get_variant(self._b, C.byref(v)), "spmv_batch_get_variant")
+        return v.as_dict()
 
     def info(self):
         t, w, n = C.c_longlong(), C.c_int(), C.c_longlong()
@@ -59,6 +67,41 @@ class BatchPlan:
             self.destroy()
         except Exception:
             pass
+
+
+def batch_variant_space(k: int) -> list[dict]:
+    """Launch shapes the batch autotuner times for k right-hand sides."""
+    out = []
+    for e in ((8, 16) if k <= 2 else (8,)):
+        for b in (2, 3):
+            for c in (1024, 2048, 4096):
+                out.append({"nnzPerSlot": e, "blocksPerSM": b, "chunkNnz": c})
+    return out
+
+
+def autotune_batch(handle: SpmvHandle, mats, k: int, xs, ys, candidates=None, repeats: int = 5,
+                   stream=None):
+    """Times each candidate variant (persistent graph launch) on this batch;
+    returns (best variant, {variant key: ms})."""
+    torch = _torch()
+    cands = candidates or batch_variant_space(k)
+    times = {}
+    for v in cands:
+        plan = BatchPlan(handle, mats, k, v)
+        plan.set_vectors(xs, ys)
+        plan.exec(1.0, 0.0, BATCH_PERSISTENT_GRAPH)
+        s = stream or torch.cuda.current_stream()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(repeats):
+            plan.exec(1.0, 0.0, BATCH_PERSISTENT_GRAPH)
+        e1.record(s)
+        e1.synchronize()
+        times[(v["nnzPerSlot"], v["blocksPerSM"], v["chunkNnz"])] = e0.elapsed_time(e1) / repeats
+        plan.destroy()
+    best = min(times, key=times.get)
+    return {"nnzPerSlot": best[0], "blocksPerSM": best[1], "chunkNnz": best[2]}, times
 
 
 def _zipf_mean(s: float, K: int) -> float:
@@ -115,5 +158,5 @@ def build_uneven_batch(count: int = 1024, k: int = 1, seed: int = 0, rmin: int =
     return mats, xs, ys, specs
 
 
-__all__ = ["BatchPlan", "uneven_specs", "build_uneven_batch", "BATCH_PERSISTENT", "BATCH_PERSISTENT_GRAPH",
+__all__ = ["BatchPlan", "uneven_specs", "build_uneven_batch", "batch_variant_space", "autotune_batch", "BATCH_PERSISTENT", "BATCH_PERSISTENT_GRAPH",
            "BATCH_LOOP", "BATCH_LOOP_GRAPH"]

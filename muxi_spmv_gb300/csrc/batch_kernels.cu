@@ -4,18 +4,20 @@
 // closest piece splits one matrix over streams, tests/test_multi_stream.cu:
 // 121-236).
 //
-// Work: every matrix is cut into tiles of 256 consecutive nonzeros (at least
-// one tile per matrix, so empty matrices still get y = beta*y).  A tile's
-// first row comes from the CSR5 tile search done once at plan creation.  One
-// persistent launch gives each warp a contiguous range of the batch's tiles
-// (equal nonzero counts per warp, whatever the matrix sizes).  Inside a tile
-// the 32 lanes form S = 32/L slots of L lanes; a slot owns 256/S consecutive
-// nonzeros and each of its lanes owns Q = min(k, 4) of the k columns, so one
-// float4 gather per lane serves a nonzero's columns (k = 16: 4 lanes x 4).
-// Rows crossing slots are joined by a segmented warp scan; a row crossing
-// tiles of the same warp is carried in registers; only the row open at the
-// end of a warp's range leaves a carry in memory, which a small fix-up kernel
-// adds in warp order -- results are deterministic and need no atomics.
+// Work: the 32 lanes of a warp form S = 32/L slots of L lanes; each lane owns
+// Q = min(k, 4) of the k columns (k = 16: 4 lanes x float4 per nonzero) and a
+// slot owns 8 consecutive nonzeros, so a tile is 8*S nonzeros (256 for k <= 4,
+// 128 for k = 8, 64 for k = 16).  Every matrix is cut into such tiles (at
+// least one, so empty matrices still get y = beta*y); a tile's first row comes
+// from the CSR5 tile search done once at plan creation.  One persistent launch
+// gives each warp a contiguous range of the batch's tiles -- equal nonzero
+// counts per warp whatever the matrix sizes -- and the warp loads tile t+1
+// (indices, values, its rowPtr slice) while it computes tile t, searching
+// rows in the slice staged in shared memory.  Rows crossing slots are joined
+// by a segmented warp scan; a row crossing tiles of the same warp is carried
+// in registers; only the row open at the end of a warp's range leaves a carry
+// in memory, which a small fix-up kernel adds in warp order -- results are
+// deterministic and need no atomics.
 #include <vector>
 
 #include "internal.h"
@@ -27,7 +29,6 @@ struct spmv_batch_s;
 
 namespace mxs {
 
-constexpr int kBatchSigma = 256;
 
 struct BatchDesc {
     const int* rowPtr;
@@ -95,59 +96,150 @@ __device__ __forceinline__ void st_yq(float* p, const float (&s)[Q], float alpha
     }
 }
 
+// Lane layout for k right-hand sides: Q columns per lane, L lanes per slot,
+// S slots per warp, E consecutive nonzeros per slot, tiles of SIGMA = E*S.
+template <int K, int E_>
+struct BatchGeom {
+    static constexpr int Q = K < 4 ? K : 4;
+    static constexpr int L = K / Q;
+    static constexpr int S = 32 / L;
+    static constexpr int E = E_;
+    static constexpr int SIGMA = E * S;
+    // rowPtr entries staged per warp: a tile without empty rows spans at
+    // most SIGMA+1 rows (SIGMA+2 entries); larger spans read rowPtr directly.
+    static constexpr int RPL = (SIGMA + 2 + 31) / 32;
+    static constexpr int CAP = 32 * RPL;
+};
+
+__host__ __device__ constexpr int batch_sigma(int k, int e) { return e * (k <= 4 ? 32 : (k == 8 ? 16 : 8)); }
+
+// Everything one tile needs from memory, loaded a tile ahead of its use.
+template <int K, int E>
+struct TileLoad {
+    int rFirst, rLast;
+    int c[E];
+    float v[E];
+    int rp[BatchGeom<K, E>::RPL];
+};
+
+template <int K, int E>
+__device__ __forceinline__ void tile_load(TileLoad<K, E>& T, const BatchDesc& d, int t, int tl, int mTileEnd,
+                                          const int* __restrict__ tileRow, int lane, int slot) {
+    using G = BatchGeom<K, E>;
+    T.rFirst = __ldg(tileRow + t);
+    T.rLast = t + 1 < mTileEnd ? __ldg(tileRow + t + 1) : d.numRows - 1;
+    const int nRp = T.rLast - T.rFirst + 2;
+#pragma unroll
+    for (int k = 0; k < G::RPL; ++k) {
+        const int i = lane + 32 * k;
+        T.rp[k] = (d.numRows > 0 && nRp <= G::CAP && i < nRp) ? __ldg(d.rowPtr + T.rFirst + i) : 0;
+    }
+    const int tStart = tl * G::SIGMA;
+    const int tEnd = min(tStart + G::SIGMA, d.nnz);
+    const int j0 = tStart + slot * E;
+    if (j0 + E <= tEnd) {
+#pragma unroll
+        for (int q = 0; q < E; q += 4) {
+            const int4 ci = ld_stream4(d.colIdx + j0 + q);
+            const float4 vi = ld_stream4(d.values + j0 + q);
+            T.c[q] = ci.x, T.c[q + 1] = ci.y, T.c[q + 2] = ci.z, T.c[q + 3] = ci.w;
+            T.v[q] = vi.x, T.v[q + 1] = vi.y, T.v[q + 2] = vi.z, T.v[q + 3] = vi.w;
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const bool in = j0 + e < tEnd;
+            T.c[e] = in ? ld_stream(d.colIdx + j0 + e) : 0;
+            T.v[e] = in ? ld_stream(d.values + j0 + e) : 0.f;
+        }
+    }
+}
+
 // tileStart[m] = first tile of matrix m (tileStart[count] = total tiles).
-// Warps of this launch split tiles [tileStart[mBegin], tileStart[mEnd]).
-template <int K>
-__global__ void __launch_bounds__(256)
+// Tiles [tileStart[mBegin], tileStart[mEnd]) form chunks of CH consecutive
+// tiles (2,048 nonzeros by default); warp w of the first numWarps takes chunks w,
+// w + numWarps, ...  so the warps in flight share a window of a few matrices
+// (their x blocks stay in L2), while rows crossing tiles of one chunk chain in
+// registers.  Each chunk leaves one carry (the row open at its end, or -1).
+template <int K, int E_, int MINB>
+__global__ void __launch_bounds__(256, MINB)
 batch_tile_kernel(const BatchDesc* __restrict__ descs, int mBegin, int mEnd, const int* __restrict__ tileStart,
                   const int* __restrict__ tileRow, int* __restrict__ carryRow, int* __restrict__ carryMat,
-                  float* __restrict__ carryVal, float alpha, float beta, int betaZero) {
-    constexpr int Q = K < 4 ? K : 4;  // columns per lane
-    constexpr int L = K / Q;          // lanes per slot
-    constexpr int S = 32 / L;         // slots per warp
-    constexpr int E = kBatchSigma / S;  // nonzeros per slot (multiple of 4)
-    static_assert(E % 4 == 0, "slot ranges must start on 16-byte boundaries");
+                  float* __restrict__ carryVal, float alpha, float beta, int betaZero, int numWarps, int CH) {
+    using G = BatchGeom<K, E_>;
+    constexpr int Q = G::Q, L = G::L, S = G::S, E = G::E, SIGMA = G::SIGMA;
+    __shared__ int sRpAll[8][G::CAP];
     const bool bz = betaZero != 0;
     const int lane = threadIdx.x & 31, slot = lane / L, kq = lane % L;
-    const long long W = (long long)gridDim.x * (blockDim.x >> 5);
-    const long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    int* sRp = sRpAll[threadIdx.x >> 5];
+    const int W = numWarps;
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (w >= W) return;  // whole warps only
     const int tAll0 = __ldg(tileStart + mBegin);
-    const long long total = (long long)__ldg(tileStart + mEnd) - tAll0;
-    const int tb = tAll0 + (int)(total * w / W), te = tAll0 + (int)(total * (w + 1) / W);
+    const int tAllEnd = __ldg(tileStart + mEnd);
+    const int chunks = (tAllEnd - tAll0 + CH - 1) / CH;
+    int ch = w;
+    if (ch >= chunks) return;
+    int t = tAll0 + ch * CH;
+    int chEnd = min(t + CH, tAllEnd);
 
-    // Matrix of the first tile: last m in [mBegin, mEnd) with tileStart[m] <= tb.
-    int m = mBegin;
+    // Matrix of the first tile: last m in [mBegin, mEnd) with tileStart[m] <= t.
+    int m;
     {
         int lo = mBegin, hi = mEnd - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (__ldg(tileStart + mid) <= tb) lo = mid;
+            if (__ldg(tileStart + mid) <= t) lo = mid;
             else hi = mid - 1;
         }
         m = lo;
     }
-    BatchDesc d = descs[m];
-    int mTile0 = __ldg(tileStart + m), mTileEnd = __ldg(tileStart + m + 1);
+    // cur = the tile being computed, nxt = the one being loaded
+    BatchDesc dCur = descs[m];
+    int mCur = m, cur0 = __ldg(tileStart + m), curEnd = __ldg(tileStart + m + 1);
+    int mNxt = mCur, nxt0 = cur0, nxtEnd = curEnd;
+    BatchDesc dNxt = dCur;
+    TileLoad<K, E> cur, nxt;
+    tile_load<K, E>(cur, dCur, t, t - cur0, curEnd, tileRow, lane, slot);
+
     int cinRow = -1;  // row carried from this warp's previous tile (same matrix)
     float cin[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) cin[q] = 0.f;
 
-    for (int t = tb; t < te; ++t) {
-        while (t >= mTileEnd) {
-            ++m;
-            d = descs[m];
-            mTile0 = mTileEnd;
-            mTileEnd = __ldg(tileStart + m + 1);
-            cinRow = -1;
+    for (;;) {
+        // the tile after this one: next in the chunk, else the warp's next chunk
+        int tn = -1, chn = ch, chEndN = chEnd;
+        if (t + 1 < chEnd) {
+            tn = t + 1;
+        } else if (ch + W < chunks) {
+            chn = ch + W;
+            tn = tAll0 + chn * CH;
+            chEndN = min(tn + CH, tAllEnd);
         }
-        const int* __restrict__ rowPtr = d.rowPtr;
-        float* __restrict__ y = d.y;
-        const int tl = t - mTile0;
-        const int tStart = tl * kBatchSigma;
-        const int tEnd = min(tStart + kBatchSigma, d.nnz);
-        const int rFirst = __ldg(tileRow + t);
-        const int rLast = t + 1 < mTileEnd ? __ldg(tileRow + t + 1) : d.numRows - 1;
+        if (tn >= 0) {
+            while (tn >= nxtEnd) {
+                ++mNxt;
+                nxt0 = nxtEnd;
+                nxtEnd = __ldg(tileStart + mNxt + 1);
+            }
+            if (mNxt != mCur) dNxt = descs[mNxt];
+            tile_load<K, E>(nxt, dNxt, tn, tn - nxt0, nxtEnd, tileRow, lane, slot);
+        }
+
+        const int* __restrict__ rowPtr = dCur.rowPtr;
+        float* __restrict__ y = dCur.y;
+        const int tl = t - cur0;
+        const int tStart = tl * SIGMA;
+        const int tEnd = min(tStart + SIGMA, dCur.nnz);
+        const int rFirst = cur.rFirst, rLast = cur.rLast;
+        const bool staged = rLast - rFirst + 2 <= G::CAP;
+        if (staged) {
+#pragma unroll
+            for (int k = 0; k < G::RPL; ++k) sRp[lane + 32 * k] = cur.rp[k];
+        }
+        __syncwarp();
+        auto RP = [&](int r) { return (staged && r >= rFirst) ? sRp[r - rFirst] : __ldg(rowPtr + r); };
         const int colOff = kq * Q;
 
         // Empty rows of (rFirst, rLast] (from row 0 in a matrix's first tile).
@@ -155,8 +247,7 @@ batch_tile_kernel(const BatchDesc* __restrict__ descs, int mBegin, int mEnd, con
             const int lo = tl == 0 ? 0 : rFirst + 1;
             const float zero[Q] = {};
             for (int r = lo + slot; r <= rLast; r += S)
-                if (__ldg(rowPtr + r) == __ldg(rowPtr + r + 1))
-                    st_yq<Q>(y + (long long)r * K + colOff, zero, alpha, beta, bz);
+                if (RP(r) == RP(r + 1)) st_yq<Q>(y + (long long)r * K + colOff, zero, alpha, beta, bz);
         }
 
         const int j0 = tStart + slot * E;
@@ -168,67 +259,48 @@ batch_tile_kernel(const BatchDesc* __restrict__ descs, int mBegin, int mEnd, con
 #pragma unroll
         for (int q = 0; q < Q; ++q) run[q] = headVal[q] = 0.f;
         if (has) {
+            // Gathers first (independent of the row search), then the search.
+            const float* __restrict__ xb = dCur.x + colOff;
+            VQ<Q> xv[E];
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                if (j0 + e < laneEnd) {
+                    xv[e] = ld_xq<Q>(xb + (long long)cur.c[e] * K);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < Q; ++q) xv[e].v[q] = 0.f;
+                }
+            }
             int lo = rFirst, hi = rLast;  // last row with rowPtr <= j0
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
-                if (__ldg(rowPtr + mid) <= j0) lo = mid;
+                if (RP(mid) <= j0) lo = mid;
                 else hi = mid - 1;
             }
             key = startRow = lo;
-            rowEnd = __ldg(rowPtr + lo + 1);
-            const float* __restrict__ xb = d.x + colOff;
-#pragma unroll 2
-            for (int e = 0; e < E; e += 4) {
-                const int j = j0 + e;
-                if (j >= laneEnd) break;
-                int c[4];
-                float v[4];
-                if (j + 4 <= laneEnd) {
-                    const int4 ci = ld_stream4(d.colIdx + j);
-                    const float4 vi = ld_stream4(d.values + j);
-                    c[0] = ci.x, c[1] = ci.y, c[2] = ci.z, c[3] = ci.w;
-                    v[0] = vi.x, v[1] = vi.y, v[2] = vi.z, v[3] = vi.w;
-                } else {
+            rowEnd = RP(lo + 1);
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const bool in = j + u < laneEnd;
-                        c[u] = in ? ld_stream(d.colIdx + j + u) : 0;
-                        v[u] = in ? ld_stream(d.values + j + u) : 0.f;
-                    }
-                }
-                VQ<Q> xv[4];
+            for (int e = 0; e < E; ++e) {
+                const int jj = j0 + e;
+                if (jj < laneEnd) {
+                    if (jj >= rowEnd) {
+                        // `key` is complete; rows skipped on the way are empty.
+                        if (headRow < 0) {
+                            headRow = key;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    if (j + u < laneEnd) {
-                        xv[u] = ld_xq<Q>(xb + (long long)c[u] * K);
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < Q; ++q) xv[u].v[q] = 0.f;
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int jj = j + u;
-                    if (jj < laneEnd) {
-                        if (jj >= rowEnd) {
-                            // `key` is complete; rows skipped on the way are empty.
-                            if (headRow < 0) {
-                                headRow = key;
-#pragma unroll
-                                for (int q = 0; q < Q; ++q) headVal[q] = run[q];
-                            } else {
-                                st_yq<Q>(y + (long long)key * K + colOff, run, alpha, beta, bz);
-                            }
-                            do {
-                                ++key;
-                                rowEnd = __ldg(rowPtr + key + 1);
-                            } while (jj >= rowEnd);
-#pragma unroll
-                            for (int q = 0; q < Q; ++q) run[q] = 0.f;
+                            for (int q = 0; q < Q; ++q) headVal[q] = run[q];
+                        } else {
+                            st_yq<Q>(y + (long long)key * K + colOff, run, alpha, beta, bz);
                         }
+                        do {
+                            ++key;
+                            rowEnd = RP(key + 1);
+                        } while (jj >= rowEnd);
 #pragma unroll
-                        for (int q = 0; q < Q; ++q) run[q] = fmaf(v[u], xv[u].v[q], run[q]);
+                        for (int q = 0; q < Q; ++q) run[q] = 0.f;
                     }
+#pragma unroll
+                    for (int q = 0; q < Q; ++q) run[q] = fmaf(cur.v[e], xv[e].v[q], run[q]);
                 }
             }
         }
@@ -286,19 +358,35 @@ batch_tile_kernel(const BatchDesc* __restrict__ descs, int mBegin, int mEnd, con
         } else {
             cinRow = -1;
         }
-    }
+        __syncwarp();  // sRp is rewritten by the next tile
 
-    if (slot == 0) {
-        if (kq == 0) {
-            carryRow[w] = cinRow;
-            carryMat[w] = m;
-        }
+        if (tn < 0 || chn != ch) {  // chunk done: leave its carry
+            if (slot == 0) {
+                if (kq == 0) {
+                    carryRow[ch] = cinRow;
+                    carryMat[ch] = mCur;
+                }
 #pragma unroll
-        for (int q = 0; q < Q; ++q) carryVal[w * K + kq * Q + q] = cin[q];
+                for (int q = 0; q < Q; ++q) carryVal[(long long)ch * K + kq * Q + q] = cin[q];
+            }
+            cinRow = -1;
+        }
+        if (tn < 0) break;
+        // advance: the loaded tile becomes the current one
+        if (mNxt != mCur) cinRow = -1;
+        t = tn;
+        ch = chn;
+        chEnd = chEndN;
+        mCur = mNxt;
+        dCur = dNxt;
+        cur0 = nxt0;
+        curEnd = nxtEnd;
+        cur = nxt;
     }
 }
 
-// Adds the carries of warps whose range ended inside a row, in warp order.
+// Adds the carries of chunks whose last tile ended inside a row, in chunk order
+// (the chunks carrying one row are consecutive: only the first adds).
 template <int K>
 __global__ void batch_fixup_kernel(const BatchDesc* __restrict__ descs, int W, const int* __restrict__ carryRow,
                                    const int* __restrict__ carryMat, const float* __restrict__ carryVal, float alpha) {
@@ -325,10 +413,13 @@ using namespace mxs;
 
 struct spmv_batch_s {
     int count = 0, k = 0, device = 0;
+    spmv_batch_variant_t variant{};
+    int sigma = 0;       // nonzeros per tile
+    int chunkTiles = 0;  // tiles per chunk of the persistent launch
     long long nnzTotal = 0;
     int tiles = 0;
-    int warps = 0;  // persistent launch: warps in the grid (= carry slots)
-    int blocksPerSM = 0;
+    int warps = 0;  // resident warps of a full-GPU launch
+    int maxTiles = 0;  // tiles of the largest matrix
     std::vector<int> hTileStart;
     std::vector<BatchDesc> hDesc;
     BatchDesc* dDesc = nullptr;
@@ -349,44 +440,59 @@ struct spmv_batch_s {
 namespace mxs {
 namespace {
 
-template <int K>
-spmv_status_t launch_range(const spmv_batch_s* b, int mBegin, int mEnd, int warps, float alpha, float beta,
+using BatchKernel = void (*)(const BatchDesc*, int, int, const int*, const int*, int*, int*, float*, float, float,
+                             int, int, int);
+using FixupKernel = void (*)(const BatchDesc*, int, const int*, const int*, const float*, float);
+
+// (k, nonzeros per slot, blocks per SM) -> kernel; nullptr where not built.
+BatchKernel batch_kernel_for(int k, int e, int minb) {
+#define MXS_BK(K, E, B) \
+    if (k == K && e == E && minb == B) return batch_tile_kernel<K, E, B>;
+    MXS_BK(1, 8, 2) MXS_BK(1, 8, 3) MXS_BK(1, 16, 2) MXS_BK(1, 16, 3)
+    MXS_BK(2, 8, 2) MXS_BK(2, 8, 3) MXS_BK(2, 16, 2) MXS_BK(2, 16, 3)
+    MXS_BK(4, 8, 2) MXS_BK(4, 8, 3)
+    MXS_BK(8, 8, 2) MXS_BK(8, 8, 3)
+    MXS_BK(16, 8, 2) MXS_BK(16, 8, 3)
+#undef MXS_BK
+    return nullptr;
+}
+
+FixupKernel fixup_kernel_for(int k) {
+    switch (k) {
+        case 1: return batch_fixup_kernel<1>;
+        case 2: return batch_fixup_kernel<2>;
+        case 4: return batch_fixup_kernel<4>;
+        case 8: return batch_fixup_kernel<8>;
+        default: return batch_fixup_kernel<16>;
+    }
+}
+
+// One launch pair over matrices [mBegin, mEnd) with chunks of chunkTiles tiles.
+spmv_status_t launch_range(const spmv_batch_s* b, int mBegin, int mEnd, int chunkTiles, float alpha, float beta,
                            cudaStream_t s) {
+    const int tiles = b->hTileStart[mEnd] - b->hTileStart[mBegin];
+    const int chunks = (tiles + chunkTiles - 1) / chunkTiles;
+    const int warps = chunks < b->warps ? chunks : b->warps;
     const int blocks = (warps + 7) / 8;
-    batch_tile_kernel<K><<<blocks, 256, 0, s>>>(b->dDesc, mBegin, mEnd, b->dTileStart, b->dTileRow, b->dCarryRow,
-                                                b->dCarryMat, b->dCarryVal, alpha, beta, beta == 0.f ? 1 : 0);
+    const BatchKernel kern = batch_kernel_for(b->k, b->variant.nnzPerSlot, b->variant.blocksPerSM);
+    kern<<<blocks, 256, 0, s>>>(b->dDesc, mBegin, mEnd, b->dTileStart, b->dTileRow, b->dCarryRow, b->dCarryMat,
+                                b->dCarryVal, alpha, beta, beta == 0.f ? 1 : 0, warps, chunkTiles);
     MXS_LAUNCH_CHECK();
-    batch_fixup_kernel<K><<<grid_for(blocks * 8, 128), 128, 0, s>>>(b->dDesc, blocks * 8, b->dCarryRow,
-                                                                     b->dCarryMat, b->dCarryVal, alpha);
+    fixup_kernel_for(b->k)<<<grid_for(chunks, 128), 128, 0, s>>>(b->dDesc, chunks, b->dCarryRow, b->dCarryMat,
+                                                                  b->dCarryVal, alpha);
     MXS_LAUNCH_CHECK();
     return SPMV_SUCCESS;
 }
 
-spmv_status_t launch_k(const spmv_batch_s* b, int mBegin, int mEnd, int warps, float alpha, float beta,
-                       cudaStream_t s) {
-    switch (b->k) {
-        case 1: return launch_range<1>(b, mBegin, mEnd, warps, alpha, beta, s);
-        case 2: return launch_range<2>(b, mBegin, mEnd, warps, alpha, beta, s);
-        case 4: return launch_range<4>(b, mBegin, mEnd, warps, alpha, beta, s);
-        case 8: return launch_range<8>(b, mBegin, mEnd, warps, alpha, beta, s);
-        case 16: return launch_range<16>(b, mBegin, mEnd, warps, alpha, beta, s);
-        default: MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "k must be 1, 2, 4, 8 or 16");
-    }
-}
-
-template <int K>
-int occupancy_blocks() {
-    int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_tile_kernel<K>, 256, 0);
-    return n > 0 ? n : 1;
-}
-
-// All launches of one execution: one persistent range, or one range per matrix.
+// All launches of one execution: one persistent range, or one range per
+// matrix (each spread over the whole GPU: chunks of ceil(tiles / warps) tiles).
 spmv_status_t launch_all(const spmv_batch_s* b, bool loop, float alpha, float beta, cudaStream_t s) {
-    if (!loop) return launch_k(b, 0, b->count, b->warps, alpha, beta, s);
+    if (!loop) return launch_range(b, 0, b->count, b->chunkTiles, alpha, beta, s);
     for (int i = 0; i < b->count; ++i) {
         const int t = b->hTileStart[i + 1] - b->hTileStart[i];
-        MXS_TRY(launch_k(b, i, i + 1, t < b->warps ? t : b->warps, alpha, beta, s));
+        int c = (t + b->warps - 1) / b->warps;
+        c = c < 1 ? 1 : (c > b->chunkTiles ? b->chunkTiles : c);
+        MXS_TRY(launch_range(b, i, i + 1, c, alpha, beta, s));
     }
     return SPMV_SUCCESS;
 }
@@ -412,8 +518,8 @@ spmv_status_t spmv_batch_destroy(spmv_batch_t b) {
     return SPMV_SUCCESS;
 }
 
-spmv_status_t spmv_batch_create(spmv_handle_t* h, int count, const spmv_batch_matrix_t* mats, int k,
-                                spmv_batch_t* out) {
+spmv_status_t spmv_batch_create_ex(spmv_handle_t* h, int count, const spmv_batch_matrix_t* mats, int k,
+                                   const spmv_batch_variant_t* variant, spmv_batch_t* out) {
     clear_error();
     if (!h) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "handle is NULL");
     if (!out) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "out is NULL");
@@ -421,7 +527,17 @@ spmv_status_t spmv_batch_create(spmv_handle_t* h, int count, const spmv_batch_ma
     if (count <= 0 || !mats) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "count must be positive and mats non-NULL");
     if (k != 1 && k != 2 && k != 4 && k != 8 && k != 16)
         MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "k must be 1, 2, 4, 8 or 16 (got %d)", k);
-    long long tiles = 0, nnzTotal = 0;
+    spmv_batch_variant_t v = variant ? *variant : spmv_batch_variant_t{};
+    if (!v.nnzPerSlot) v.nnzPerSlot = 8;
+    if (!v.blocksPerSM) v.blocksPerSM = 2;
+    if (!v.chunkNnz) v.chunkNnz = 2048;
+    if (!batch_kernel_for(k, v.nnzPerSlot, v.blocksPerSM))
+        MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "no batch kernel for k=%d, %d nonzeros per slot, %d blocks per SM", k,
+                 v.nnzPerSlot, v.blocksPerSM);
+    const int sigma = batch_sigma(k, v.nnzPerSlot);
+    if (v.chunkNnz < sigma || v.chunkNnz % sigma)
+        MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "chunkNnz must be a positive multiple of the tile (%d)", sigma);
+    long long tiles = 0, nnzTotal = 0, maxTiles = 0;
     std::vector<int> tileStart(count + 1);
     for (int i = 0; i < count; ++i) {
         const spmv_batch_matrix_t& a = mats[i];
@@ -435,7 +551,9 @@ spmv_status_t spmv_batch_create(spmv_handle_t* h, int count, const spmv_batch_ma
         if (a.nnz > 0 && (!aligned(a.colIdx, 16) || !aligned(a.values, 16)))
             MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "matrix %d: colIdx and values must be 16-byte aligned", i);
         tileStart[i] = (int)tiles;
-        tiles += a.nnz > 0 ? ((long long)a.nnz + kBatchSigma - 1) / kBatchSigma : 1;
+        const long long mt = a.nnz > 0 ? ((long long)a.nnz + sigma - 1) / sigma : 1;
+        tiles += mt;
+        if (mt > maxTiles) maxTiles = mt;
         nnzTotal += a.nnz;
         if (tiles > 0x7fffffff - 1) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "batch has more than 2^31 tiles");
     }
@@ -445,22 +563,21 @@ spmv_status_t spmv_batch_create(spmv_handle_t* h, int count, const spmv_batch_ma
     if (!b) MXS_FAIL(SPMV_ERROR_MEMORY_ALLOC, "out of host memory");
     b->count = count;
     b->k = k;
+    b->variant = v;
+    b->sigma = sigma;
+    b->chunkTiles = v.chunkNnz / sigma;
     b->device = h->deviceId;
     b->tiles = (int)tiles;
+    b->maxTiles = (int)maxTiles;
     b->nnzTotal = nnzTotal;
     b->hTileStart = tileStart;
     b->hDesc.resize(count);
     for (int i = 0; i < count; ++i)
         b->hDesc[i] = BatchDesc{mats[i].rowPtr, mats[i].colIdx, mats[i].values, nullptr, nullptr, mats[i].numRows,
                                 mats[i].nnz};
-    switch (k) {
-        case 1: b->blocksPerSM = occupancy_blocks<1>(); break;
-        case 2: b->blocksPerSM = occupancy_blocks<2>(); break;
-        case 4: b->blocksPerSM = occupancy_blocks<4>(); break;
-        case 8: b->blocksPerSM = occupancy_blocks<8>(); break;
-        default: b->blocksPerSM = occupancy_blocks<16>(); break;
-    }
-    b->warps = current_sm_count() * b->blocksPerSM * 8;
+    int perSM = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, batch_kernel_for(k, v.nnzPerSlot, v.blocksPerSM), 256, 0);
+    b->warps = current_sm_count() * (perSM > 0 ? perSM : 1) * 8;
 
     const cudaStream_t s = h->stream;
     int* tileOff = nullptr;
@@ -469,17 +586,20 @@ spmv_status_t spmv_batch_create(spmv_handle_t* h, int count, const spmv_batch_ma
     if (e == cudaSuccess) e = cudaMalloc(&b->dTileStart, sizeof(int) * (count + 1));
     if (e == cudaSuccess) e = cudaMalloc(&b->dTileRow, sizeof(int) * tiles);
     if (e == cudaSuccess) e = cudaMalloc(&tileOff, sizeof(int) * tiles);
-    // carries: row, matrix, k values per warp slot
-    const size_t cb = ((sizeof(int) * 2 * b->warps + 255) & ~size_t(255)) + sizeof(float) * k * (size_t)b->warps;
+    // carries: row, matrix, k values per chunk
+    // persistent chunks, or at most one full-GPU grid of chunks per matrix
+    size_t nch = (size_t)((tiles + b->chunkTiles - 1) / b->chunkTiles);
+    if (nch < (size_t)b->warps) nch = (size_t)b->warps;
+    const size_t rowsBytes = (sizeof(int) * 2 * nch + 255) & ~size_t(255);
+    const size_t cb = rowsBytes + sizeof(float) * k * nch;
     if (e == cudaSuccess) e = cudaMalloc(&b->dCarryRow, cb);
     if (e != cudaSuccess) {
         cudaFree(tileOff);
         spmv_batch_destroy(b);
         return cuda_fail(e, "batch allocation", __FILE__, __LINE__);
     }
-    b->dCarryMat = b->dCarryRow + b->warps;
-    b->dCarryVal = reinterpret_cast<float*>(reinterpret_cast<char*>(b->dCarryRow) +
-                                            ((sizeof(int) * 2 * b->warps + 255) & ~size_t(255)));
+    b->dCarryMat = b->dCarryRow + nch;
+    b->dCarryVal = reinterpret_cast<float*>(reinterpret_cast<char*>(b->dCarryRow) + rowsBytes);
     e = cudaMemcpyAsync(b->dTileStart, tileStart.data(), sizeof(int) * (count + 1), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->dTileRow, 0, sizeof(int) * tiles, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->dDesc, b->hDesc.data(), sizeof(BatchDesc) * count,
@@ -487,7 +607,7 @@ spmv_status_t spmv_batch_create(spmv_handle_t* h, int count, const spmv_batch_ma
     if (e != cudaSuccess) st = cuda_fail(e, "batch setup", __FILE__, __LINE__);
     for (int i = 0; i < count && st == SPMV_SUCCESS; ++i)
         if (mats[i].nnz > 0)
-            st = csr5_tiles(mats[i].rowPtr, mats[i].numRows, mats[i].nnz, kBatchSigma, b->dTileRow + tileStart[i],
+            st = csr5_tiles(mats[i].rowPtr, mats[i].numRows, mats[i].nnz, sigma, b->dTileRow + tileStart[i],
                             tileOff + tileStart[i], s);
     if (st == SPMV_SUCCESS) {
         e = cudaStreamSynchronize(s);
@@ -499,6 +619,18 @@ spmv_status_t spmv_batch_create(spmv_handle_t* h, int count, const spmv_batch_ma
         return st;
     }
     *out = b;
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_batch_create(spmv_handle_t* h, int count, const spmv_batch_matrix_t* mats, int k,
+                                spmv_batch_t* out) {
+    return spmv_batch_create_ex(h, count, mats, k, nullptr, out);
+}
+
+spmv_status_t spmv_batch_get_variant(spmv_batch_t b, spmv_batch_variant_t* v) {
+    clear_error();
+    if (!b || !v) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "NULL argument");
+    *v = b->variant;
     return SPMV_SUCCESS;
 }
 

@@ -147,3 +147,28 @@ def test_uneven_batch_small_sample(mx, cuda, handle):
         for j in range(4):
             yr, absum = oracle.spmv_ref(rp, ci, v, np.ascontiguousarray(X[:, j]))
             assert (np.abs(Y[:, j] - yr) <= 1e-5 * absum).all()
+
+
+@pytest.mark.parametrize("k,variant", [(1, {"nnzPerSlot": 16, "blocksPerSM": 2, "chunkNnz": 1024}),
+                                       (2, {"nnzPerSlot": 16, "blocksPerSM": 3, "chunkNnz": 4096}),
+                                       (1, {"nnzPerSlot": 8, "blocksPerSM": 3, "chunkNnz": 256}),
+                                       (16, {"nnzPerSlot": 8, "blocksPerSM": 3, "chunkNnz": 64})])
+def test_batch_variants_match_oracle(mx, cuda, handle, hbatch, dmats, k, variant):
+    from muxi_spmv_gb300 import batch as B
+    rng = np.random.default_rng(100 + k)
+    X = [rng.uniform(-1, 1, c * k).astype(np.float32) for (_, _, _, c) in hbatch]
+    Y0 = [rng.uniform(-1, 1, (len(rp) - 1) * k).astype(np.float32) for (rp, _, _, _) in hbatch]
+    dX = [cuda.from_numpy(x).cuda() for x in X]
+    plan = B.BatchPlan(handle, dmats, k, variant)
+    assert plan.variant == variant
+    for mode in (B.BATCH_PERSISTENT_GRAPH, B.BATCH_LOOP):
+        dY = [cuda.from_numpy(y0.copy()).cuda() if y0.size else cuda.zeros(4, device="cuda") for y0 in Y0]
+        plan.set_vectors(dX, dY)
+        plan.exec(0.75, 0.25, mode)
+        cuda.cuda.synchronize()
+        _check(hbatch, X, Y0, [y.cpu().numpy()[:y0.size] for y, y0 in zip(dY, Y0)], k, 0.75, 0.25)
+    plan.destroy()
+    with pytest.raises(mx.SpmvError):
+        B.BatchPlan(handle, dmats, 4, {"nnzPerSlot": 16})  # not built for k = 4
+    with pytest.raises(mx.SpmvError):
+        B.BatchPlan(handle, dmats, 1, {"chunkNnz": 300})  # not a multiple of the tile
