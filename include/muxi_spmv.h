@@ -197,9 +197,15 @@ typedef enum {
 typedef struct {
     spmv_kernel_t kernel;
     int blockSize;       /* threads per CTA: 128, 256 or 512               */
-    int threadsPerRow;   /* VECTOR: 1,2,4,8,16,32                          */
-    int itemsPerThread;  /* MERGE: merge items per thread (tile = block*ipt) */
-    int vectorWidth;     /* VECTOR/ELL: 1 or 4 elements per load           */
+    int threadsPerRow;   /* VECTOR: 1,2,4,8,16,32; CSR5 with vectorWidth 32:
+                            tiles per chunk of a persistent launch (blocks
+                            of blockSize 256/512/1024 threads take chunks
+                            in turn), 0 = one tile per warp               */
+    int itemsPerThread;  /* MERGE: merge items per thread (tile = block*ipt);
+                            CSR5/BAND: nonzeros per lane (tile = 32*ipt)   */
+    int vectorWidth;     /* VECTOR/MERGE: 1 or 4 elements per load;
+                            CSR5: 32 = gathers issued in nonzero order
+                            (32 consecutive nonzeros per instruction)      */
 } spmv_variant_t;
 
 /* Run one explicit variant (no plan, no selector).  MERGE variants take
@@ -572,10 +578,11 @@ typedef enum {
     SPMV_BATCH_LOOP_GRAPH = 3         /* the per-matrix loop replayed from a graph  */
 } spmv_batch_mode_t;
 
-/* Launch shape of a batch (0 in a field = its default): nonzeros per slot
- * of 8 lanes' work (8, or 16 for k <= 2; default 8), resident blocks per SM
- * the kernel is compiled for (2 or 3; default 2), and nonzeros per work
- * chunk handed to a warp (a multiple of the tile; default 2048). */
+/* Launch shape of a batch (0 in a field = its default): consecutive
+ * nonzeros per slot of lanes (8, or 4; default 8), resident 256-thread blocks
+ * per SM the kernel is compiled for (2; 3 with 4 nonzeros per slot; default
+ * 2), and nonzeros per work chunk handed to a warp (a multiple of the tile,
+ * which is nnzPerSlot * 32 / (k/4 rounded up to 1); default 2048). */
 typedef struct {
     int nnzPerSlot;
     int blocksPerSM;

@@ -72,10 +72,9 @@ class BatchPlan:
 def batch_variant_space(k: int) -> list[dict]:
     """Launch shapes the batch autotuner times for k right-hand sides."""
     out = []
-    for e in ((8, 16) if k <= 2 else (8,)):
-        for b in (2, 3):
-            for c in (1024, 2048, 4096):
-                out.append({"nnzPerSlot": e, "blocksPerSM": b, "chunkNnz": c})
+    for e, b in ((8, 2), (4, 2), (4, 3)):
+        for c in (1024, 2048, 4096):
+            out.append({"nnzPerSlot": e, "blocksPerSM": b, "chunkNnz": c})
     return out
 
 

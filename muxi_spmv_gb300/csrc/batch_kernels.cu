@@ -448,11 +448,11 @@ using FixupKernel = void (*)(const BatchDesc*, int, const int*, const int*, cons
 BatchKernel batch_kernel_for(int k, int e, int minb) {
 #define MXS_BK(K, E, B) \
     if (k == K && e == E && minb == B) return batch_tile_kernel<K, E, B>;
-    MXS_BK(1, 8, 2) MXS_BK(1, 8, 3) MXS_BK(1, 16, 2) MXS_BK(1, 16, 3)
-    MXS_BK(2, 8, 2) MXS_BK(2, 8, 3) MXS_BK(2, 16, 2) MXS_BK(2, 16, 3)
-    MXS_BK(4, 8, 2) MXS_BK(4, 8, 3)
-    MXS_BK(8, 8, 2) MXS_BK(8, 8, 3)
-    MXS_BK(16, 8, 2) MXS_BK(16, 8, 3)
+    MXS_BK(1, 8, 2) MXS_BK(1, 4, 2) MXS_BK(1, 4, 3)
+    MXS_BK(2, 8, 2) MXS_BK(2, 4, 2) MXS_BK(2, 4, 3)
+    MXS_BK(4, 8, 2) MXS_BK(4, 4, 2) MXS_BK(4, 4, 3)
+    MXS_BK(8, 8, 2) MXS_BK(8, 4, 2) MXS_BK(8, 4, 3)
+    MXS_BK(16, 8, 2) MXS_BK(16, 4, 2) MXS_BK(16, 4, 3)
 #undef MXS_BK
     return nullptr;
 }

@@ -64,14 +64,14 @@ __device__ __forceinline__ void csr5_load(Csr5Load<T, E>& L, long long t, int la
     }
 }
 
-// sRp: this warp's shared-memory region of csr5_rp_cap<E>() ints.
-// The tile logic proper.  c/v: this lane's E column indices and values;
-// RP(r): rowPtr[r] for r in [0, rLast+1]; gather(c): x[c].
-template <typename T, int E, typename RowPtrAt, typename Gather>
-__device__ __forceinline__ void csr5_tile_core(const int (&cIdx)[E], const T (&vals)[E], int rFirst, int rLast,
-                                               long long t, int lane, int nnz, T* __restrict__ y, T alpha, T beta,
-                                               bool bz, int* __restrict__ carryRow, T* __restrict__ carryVal,
-                                               RowPtrAt RP, Gather gather) {
+// The row logic of a tile over this lane's E products p[e] = a_j * x[col_j]
+// (zero past the tile end); RP(r): rowPtr[r] for r in [0, rLast+1].
+// noEmpty: the caller knows every row holds a nonzero (no empty-row pass).
+template <typename T, int E, typename RowPtrAt>
+__device__ __forceinline__ void csr5_tile_rows(const T (&p)[E], int rFirst, int rLast, long long t, int lane, int nnz,
+                                               T* __restrict__ y, T alpha, T beta, bool bz,
+                                               int* __restrict__ carryRow, T* __restrict__ carryVal, RowPtrAt RP,
+                                               bool noEmpty = false) {
     // 32-bit positions: the plans that run these tiles require
     // nnz <= INT_MAX - 32*E*32, so no position below overflows.
     constexpr int SIGMA = 32 * E;
@@ -79,7 +79,7 @@ __device__ __forceinline__ void csr5_tile_core(const int (&cIdx)[E], const T (&v
     const int tEnd = min(tStart + SIGMA, nnz);
 
     // Empty rows of this tile's range: (rFirst, rLast], plus leading rows for tile 0.
-    {
+    if (!noEmpty) {
         const int lo = t == 0 ? 0 : rFirst + 1;
         for (int r = lo + lane; r <= rLast; r += 32)
             if (RP(r) == RP(r + 1)) y[r] = bz ? T(0) : beta * y[r];
@@ -94,9 +94,6 @@ __device__ __forceinline__ void csr5_tile_core(const int (&cIdx)[E], const T (&v
     int headRow = -1, startRow = -1;
     int rowEnd = 0;
     if (has) {
-        T p[E];
-#pragma unroll
-        for (int e = 0; e < E; ++e) p[e] = j0 + e < laneEnd ? vals[e] * gather(cIdx[e]) : T(0);
         int lo = rFirst, hi = rLast;  // last row with rowPtr <= j0
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
@@ -145,6 +142,22 @@ __device__ __forceinline__ void csr5_tile_core(const int (&cIdx)[E], const T (&v
         carryRow[t] = rowEnd > laneEnd ? key : -1;
         carryVal[t] = incl;
     }
+}
+
+// The tile logic with the products formed here.  c/v: this lane's E column
+// indices and values; gather(c): x[c].
+template <typename T, int E, typename RowPtrAt, typename Gather>
+__device__ __forceinline__ void csr5_tile_core(const int (&cIdx)[E], const T (&vals)[E], int rFirst, int rLast,
+                                               long long t, int lane, int nnz, T* __restrict__ y, T alpha, T beta,
+                                               bool bz, int* __restrict__ carryRow, T* __restrict__ carryVal,
+                                               RowPtrAt RP, Gather gather) {
+    constexpr int SIGMA = 32 * E;
+    const int j0 = (int)t * SIGMA + lane * E;
+    const int laneEnd = min(j0 + E, min((int)t * SIGMA + SIGMA, nnz));
+    T p[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) p[e] = j0 + e < laneEnd ? vals[e] * gather(cIdx[e]) : T(0);
+    csr5_tile_rows<T, E>(p, rFirst, rLast, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal, RP);
 }
 
 // Tile with register-loaded data (csr5_load): stages the rowPtr slice in this

@@ -41,6 +41,172 @@ csr5_tile_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int
                        sRp[threadIdx.x >> 5], [x](int c) { return ld_x(x + c); });
 }
 
+// CSR5 tiles with the gathers issued in nonzero order: lane l loads nonzeros
+// t*32E + l + 32e (every load instruction covers 32 consecutive nonzeros, so
+// x gathers of consecutive columns share sectors).
+//   * A tile strictly inside one row (tile_row_ptr[t] == tile_row_ptr[t+1]:
+//     no row starts in it, the row runs on past its end) -- most tiles of
+//     long rows -- needs no row logic: a warp sum of its products becomes the
+//     tile's carry.
+//   * Any other tile hands each lane its E consecutive products through
+//     shared memory and runs the CSR5 row logic.
+// sRp / sP: this warp's shared regions (csr5_rp_cap<E>() ints, 32E values).
+template <typename T, int E>
+struct OrderedLoad {
+    int rFirst, rLast;
+    int c[E];
+    T v[E];
+};
+
+template <typename T, int E>
+__device__ __forceinline__ void csr5_ordered_load(OrderedLoad<T, E>& L, long long t, int lane, int numRows, int nnz,
+                                                  const int* __restrict__ colIdx, const T* __restrict__ values,
+                                                  const int* __restrict__ tileRow, long long tiles) {
+    constexpr int SIGMA = 32 * E;
+    const int tStart = (int)t * SIGMA;
+    if (tStart + SIGMA <= nnz) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            L.c[e] = ld_stream(colIdx + tStart + lane + 32 * e);
+            L.v[e] = ld_stream(values + tStart + lane + 32 * e);
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const int j = tStart + lane + 32 * e;
+            L.c[e] = j < nnz ? ld_stream(colIdx + j) : 0;
+            L.v[e] = j < nnz ? ld_stream(values + j) : T(0);
+        }
+    }
+    L.rFirst = __ldg(tileRow + t);
+    L.rLast = t + 1 < tiles ? __ldg(tileRow + t + 1) : numRows - 1;
+}
+
+// REUSE: the warp runs further tiles on the same shared regions afterwards.
+template <typename T, int E, bool REUSE>
+__device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L, long long t, int lane, int nnz,
+                                                     const int* __restrict__ rowPtr, const T* __restrict__ x,
+                                                     T* __restrict__ y, T alpha, T beta, bool bz, long long tiles,
+                                                     int* __restrict__ carryRow, T* __restrict__ carryVal,
+                                                     bool noEmpty, int* sRp, T* sP) {
+    const int rFirst = L.rFirst, rLast = L.rLast;
+    T g[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) g[e] = ld_x(x + L.c[e]);  // past nnz: c = 0, v = 0, unused
+
+    if (rFirst == rLast && t + 1 < tiles) {  // interior tile of one row
+        T sum = T(0);
+#pragma unroll
+        for (int e = 0; e < E; ++e) sum += L.v[e] * g[e];
+        sum = group_sum<32>(sum);
+        if (lane == 0) {
+            carryRow[t] = rFirst;
+            carryVal[t] = sum;
+        }
+        return;
+    }
+
+    const int nRp = rLast - rFirst + 2;
+    const bool staged = nRp <= csr5_rp_cap<E>();
+    if (staged) {
+#pragma unroll
+        for (int k = 0; k < csr5_rp_per_lane<E>(); ++k) {
+            const int i = lane + 32 * k;
+            if (i < nRp) sRp[i] = __ldg(rowPtr + rFirst + i);
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e) sP[lane + 32 * e] = L.v[e] * g[e];
+    __syncwarp();
+    T p[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) p[e] = sP[lane * E + e];
+    csr5_tile_rows<T, E>(p, rFirst, rLast, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal,
+                         [&](int r) { return (staged && r >= rFirst) ? sRp[r - rFirst] : __ldg(rowPtr + r); },
+                         noEmpty);
+    if (REUSE) __syncwarp();  // the regions are reused by this warp's next tile
+}
+
+template <typename T, int E>
+__device__ __forceinline__ void csr5_ordered_tile(long long t, int lane, int numRows, int nnz,
+                                                  const int* __restrict__ rowPtr, const int* __restrict__ colIdx,
+                                                  const T* __restrict__ values, const T* __restrict__ x,
+                                                  T* __restrict__ y, T alpha, T beta, bool bz,
+                                                  const int* __restrict__ tileRow, long long tiles,
+                                                  int* __restrict__ carryRow, T* __restrict__ carryVal, bool noEmpty,
+                                                  int* sRp, T* sP) {
+    OrderedLoad<T, E> L;
+    csr5_ordered_load<T, E>(L, t, lane, numRows, nnz, colIdx, values, tileRow, tiles);
+    csr5_ordered_compute<T, E, false>(L, t, lane, nnz, rowPtr, x, y, alpha, beta, bz, tiles, carryRow, carryVal,
+                                      noEmpty, sRp, sP);
+}
+
+// One tile per warp, BLOCK threads per block, MINB resident blocks per SM
+// (the launch bound sets the register budget: 128x16 and 512x4 keep 64 warps
+// per SM at 32 registers, 256x6 keeps 48 at 40).
+template <typename T, int E, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB)
+csr5_ordered_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int* __restrict__ colIdx,
+                    const T* __restrict__ values, const T* __restrict__ x, T* __restrict__ y, T alpha, T beta,
+                    int betaZero, const int* __restrict__ tileRow, long long tiles, int* __restrict__ carryRow,
+                    T* __restrict__ carryVal, int noEmptyRows) {
+    constexpr int WARPS = BLOCK / 32;
+    __shared__ int sRpAll[WARPS][csr5_rp_cap<E>()];
+    __shared__ __align__(16) T sPAll[WARPS][32 * E];
+    const long long t = ((long long)blockIdx.x * BLOCK + threadIdx.x) >> 5;
+    if (t >= tiles) return;  // uniform per warp
+    const int w = threadIdx.x >> 5;
+    csr5_ordered_tile<T, E>(t, threadIdx.x & 31, numRows, nnz, rowPtr, colIdx, values, x, y, alpha, beta,
+                            betaZero != 0, tileRow, tiles, carryRow, carryVal, noEmptyRows != 0, sRpAll[w], sPAll[w]);
+}
+
+// Persistent: block b takes chunks b, b + gridDim.x, ... of `chunk`
+// consecutive tiles, its WARPS warps taking a chunk's tiles in turn (the
+// warps of an SM work on neighbouring rows, so the near-diagonal x they gather
+// stays in that SM's L1).  Each warp loads its next tile while it computes
+// the current one.
+template <typename T, int E, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+csr5_ordered_persistent_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int* __restrict__ colIdx,
+                               const T* __restrict__ values, const T* __restrict__ x, T* __restrict__ y, T alpha,
+                               T beta, int betaZero, const int* __restrict__ tileRow, long long tiles,
+                               int* __restrict__ carryRow, T* __restrict__ carryVal, int noEmptyRows, int chunk) {
+    __shared__ int sRpAll[WARPS][csr5_rp_cap<E>()];
+    __shared__ __align__(16) T sPAll[WARPS][32 * E];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // Tile and chunk counts fit in int: plans cap nnz below 2^31.
+    const int ntiles = (int)tiles;
+    const int chunks = (ntiles + chunk - 1) / chunk;
+    // this warp's tiles: ch*chunk + w + i*WARPS inside chunk ch, for chunks
+    // ch = blockIdx.x, blockIdx.x + gridDim.x, ...
+    int ch = blockIdx.x, t = -1;
+    for (; ch < chunks; ch += gridDim.x) {
+        t = ch * chunk + w;
+        if (t < ntiles && t < ch * chunk + chunk) break;
+        t = -1;
+    }
+    if (t < 0) return;
+    OrderedLoad<T, E> cur, nxt;
+    csr5_ordered_load<T, E>(cur, t, lane, numRows, nnz, colIdx, values, tileRow, tiles);
+    while (t >= 0) {
+        int tn = t + WARPS, chn = ch;
+        if (tn >= ntiles || tn >= ch * chunk + chunk) {
+            tn = -1;
+            for (chn = ch + gridDim.x; chn < chunks; chn += gridDim.x) {
+                tn = chn * chunk + w;
+                if (tn < ntiles && tn < chn * chunk + chunk) break;
+                tn = -1;
+            }
+        }
+        if (tn >= 0) csr5_ordered_load<T, E>(nxt, tn, lane, numRows, nnz, colIdx, values, tileRow, tiles);
+        csr5_ordered_compute<T, E, true>(cur, t, lane, nnz, rowPtr, x, y, alpha, beta, betaZero != 0, tiles,
+                                         carryRow, carryVal, noEmptyRows != 0, sRpAll[w], sPAll[w]);
+        cur = nxt;
+        t = tn;
+        ch = chn;
+    }
+}
+
 // Adds each split row's carries in tile order (rows with carry -1 skipped).
 template <typename T>
 __global__ void csr5_fixup_kernel(long long tiles, const int* __restrict__ carryRow, const T* __restrict__ carryVal,
@@ -55,21 +221,74 @@ __global__ void csr5_fixup_kernel(long long tiles, const int* __restrict__ carry
     y[r] += alpha * s;
 }
 
+template <typename T, int E, int WARPS>
+static spmv_status_t launch_ordered_persistent(const int* tileRow, long long tiles, int* carryRow, T* carryVal,
+                                               const RowsArgs<T>& a, int chunk, cudaStream_t s) {
+    static int perSM = -1;  // resident blocks per SM of this instantiation
+    if (perSM < 0) {
+        int n = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, csr5_ordered_persistent_kernel<T, E, WARPS>, WARPS * 32, 0);
+        perSM = n > 0 ? n : 1;
+    }
+    const long long chunks = (tiles + chunk - 1) / chunk;
+    long long g = (long long)current_sm_count() * perSM;
+    if (g > chunks) g = chunks;
+    csr5_ordered_persistent_kernel<T, E, WARPS><<<(unsigned)g, WARPS * 32, 0, s>>>(
+        a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha, a.beta, a.betaZero, tileRow, tiles,
+        carryRow, carryVal, a.noEmptyRows, chunk);
+    return SPMV_SUCCESS;
+}
+
+template <typename T, int E>
+static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* carryRow, T* carryVal,
+                                    const RowsArgs<T>& a, int block, int chunk, cudaStream_t s) {
+    if (chunk <= 0) {
+        constexpr bool wide = E * sizeof(T) >= 64;  // 16 doubles or floats per lane: fewer, larger blocks
+#define MXS_ORDERED(B, M)                                                                                        \
+    csr5_ordered_kernel<T, E, B, M><<<grid_for(tiles * 32, B), B, 0, s>>>(                                        \
+        a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha, a.beta, a.betaZero, tileRow, tiles,   \
+        carryRow, carryVal, a.noEmptyRows)
+        switch (block) {
+            case 128: MXS_ORDERED(128, wide ? 6 : 16); break;
+            case 256: MXS_ORDERED(256, wide ? 3 : 6); break;
+            case 512: MXS_ORDERED(512, wide ? 2 : 4); break;
+            default: MXS_FAIL(SPMV_ERROR_INTERNAL, "ordered CSR5 block must be 128, 256 or 512 (got %d)", block);
+        }
+#undef MXS_ORDERED
+        return SPMV_SUCCESS;
+    }
+    switch (block) {
+        case 256: return launch_ordered_persistent<T, E, 8>(tileRow, tiles, carryRow, carryVal, a, chunk, s);
+        case 512: return launch_ordered_persistent<T, E, 16>(tileRow, tiles, carryRow, carryVal, a, chunk, s);
+        case 1024: return launch_ordered_persistent<T, E, 32>(tileRow, tiles, carryRow, carryVal, a, chunk, s);
+        default: MXS_FAIL(SPMV_ERROR_INTERNAL, "persistent CSR5 block must be 256, 512 or 1024 (got %d)", block);
+    }
+}
+
 template <typename T>
 spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
-                       const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain) {
-    const unsigned g = grid_for(tiles * 32, 256);
-    if (sigma == 128) {
-        csr5_tile_kernel<T, 4><<<g, 256, 0, s>>>(a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha,
-                                                 a.beta, a.betaZero, tileRow, tiles, carryRow, carryVal);
-    } else if (sigma == 256) {
-        csr5_tile_kernel<T, 8><<<g, 256, 0, s>>>(a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha,
-                                                 a.beta, a.betaZero, tileRow, tiles, carryRow, carryVal);
-    } else if (sigma == 512) {
-        csr5_tile_kernel<T, 16><<<g, 256, 0, s>>>(a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha,
-                                                  a.beta, a.betaZero, tileRow, tiles, carryRow, carryVal);
+                       const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain, bool ordered, int block,
+                       int chunk) {
+    if (ordered) {
+        if (sigma == 128) MXS_TRY((launch_ordered<T, 4>(tileRow, tiles, carryRow, carryVal, a, block, chunk, s)));
+        else if (sigma == 256) MXS_TRY((launch_ordered<T, 8>(tileRow, tiles, carryRow, carryVal, a, block, chunk, s)));
+        else if (sigma == 512) MXS_TRY((launch_ordered<T, 16>(tileRow, tiles, carryRow, carryVal, a, block, chunk, s)));
+        else MXS_FAIL(SPMV_ERROR_INTERNAL, "CSR5 sigma must be 128, 256 or 512 (got %d)", sigma);
     } else {
-        MXS_FAIL(SPMV_ERROR_INTERNAL, "CSR5 sigma must be 128, 256 or 512 (got %d)", sigma);
+        const unsigned g = grid_for(tiles * 32, 256);
+        if (sigma == 128) {
+            csr5_tile_kernel<T, 4><<<g, 256, 0, s>>>(a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y,
+                                                     a.alpha, a.beta, a.betaZero, tileRow, tiles, carryRow, carryVal);
+        } else if (sigma == 256) {
+            csr5_tile_kernel<T, 8><<<g, 256, 0, s>>>(a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y,
+                                                     a.alpha, a.beta, a.betaZero, tileRow, tiles, carryRow, carryVal);
+        } else if (sigma == 512) {
+            csr5_tile_kernel<T, 16><<<g, 256, 0, s>>>(a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y,
+                                                      a.alpha, a.beta, a.betaZero, tileRow, tiles, carryRow,
+                                                      carryVal);
+        } else {
+            MXS_FAIL(SPMV_ERROR_INTERNAL, "CSR5 sigma must be 128, 256 or 512 (got %d)", sigma);
+        }
     }
     MXS_LAUNCH_CHECK();
     if (afterMain) MXS_CUDA(cudaEventRecord(afterMain, s));
@@ -88,9 +307,9 @@ template spmv_status_t run_csr5_fixup<float>(long long, const int*, const float*
 template spmv_status_t run_csr5_fixup<double>(long long, const int*, const double*, const RowsArgs<double>&,
                                               cudaStream_t);
 template spmv_status_t run_csr5<float>(int, const int*, long long, int*, float*, const RowsArgs<float>&,
-                                       cudaStream_t, cudaEvent_t);
+                                       cudaStream_t, cudaEvent_t, bool, int, int);
 template spmv_status_t run_csr5<double>(int, const int*, long long, int*, double*, const RowsArgs<double>&,
-                                        cudaStream_t, cudaEvent_t);
+                                        cudaStream_t, cudaEvent_t, bool, int, int);
 
 // ---------------------------------------------------------------------------
 // ELL

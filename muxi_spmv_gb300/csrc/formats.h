@@ -7,9 +7,13 @@
 namespace mxs {
 
 // Tile kernel then carry fix-up; carryRow/carryVal hold `tiles` entries.
+// ordered: gathers issued in nonzero order (csr5_ordered_kernel); with
+// chunk > 0 the ordered tiles run persistently, blocks of `block` threads
+// taking chunks of `chunk` consecutive tiles.
 template <typename T>
 spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
-                       const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain = nullptr);
+                       const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain = nullptr, bool ordered = false,
+                       int block = 256, int chunk = 0);
 
 // Adds the carries of rows split between CSR5 tiles, in tile order.
 template <typename T>

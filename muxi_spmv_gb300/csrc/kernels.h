@@ -18,6 +18,7 @@ struct RowsArgs {
     T alpha;
     T beta;
     int betaZero;
+    int noEmptyRows = 0;  // set by plans that checked every row holds a nonzero
 };
 
 // Scalar / vector CSR kernels (csr_kernels.cu).

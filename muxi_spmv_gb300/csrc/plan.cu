@@ -30,11 +30,12 @@ static spmv_variant_t resolve(const spmv_variant_t* req, int R, int N) {
     if (req) v = *req;
     if (v.kernel == SPMV_KERNEL_HEURISTIC) return heuristic_variant(R, N);
     if (v.kernel == SPMV_KERNEL_AUTO) {
-        // Without a selector model: CSR5 tiles of 256 nonzeros (nnz-balanced,
-        // warp-local, the fastest measured variant on irregular matrices);
-        // merge-path tiles when the nonzero count is beyond CSR5's range.
+        // Without a selector model: CSR5 tiles of 256 nonzeros with gathers in
+        // nonzero order, 128-thread blocks (nnz-balanced, warp-local, the
+        // fastest measured variant on irregular matrices); merge-path tiles
+        // when the nonzero count is beyond CSR5's range.
         if (N > 0x7fffffff - 32768) return spmv_variant_t{SPMV_KERNEL_MERGE, 256, 0, 8, 4};
-        return spmv_variant_t{SPMV_KERNEL_CSR5, 256, 0, 8, 1};
+        return spmv_variant_t{SPMV_KERNEL_CSR5, 128, 0, 8, 32};
     }
     if (!v.blockSize) v.blockSize = 256;
     if (v.kernel == SPMV_KERNEL_SCALAR) v.threadsPerRow = 1;
@@ -60,6 +61,7 @@ static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T
     if (p->nnz == 0) return run_scale<T>(p->numRows, y, beta, s);
     RowsArgs<T> a{p->numRows, p->nnz, p->rowPtr, p->colIdx, static_cast<const T*>(p->values), x, y,
                   alpha, beta, beta == T(0)};
+    a.noEmptyRows = p->noEmptyRows ? 1 : 0;
     const spmv_variant_t& v = p->variant;
     cudaEvent_t evStart = nullptr, evEnd = nullptr;
     if (p->profiling) {
@@ -89,7 +91,8 @@ static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T
             break;
         case SPMV_KERNEL_CSR5:
             MXS_TRY(run_csr5<T>(32 * v.itemsPerThread, p->csr5TileRow, p->csr5Tiles, p->csr5CarryRow,
-                                static_cast<T*>(p->csr5CarryVal), a, s, evEnd));
+                                static_cast<T*>(p->csr5CarryVal), a, s, evEnd, v.vectorWidth == 32, v.blockSize,
+                                v.vectorWidth == 32 ? v.threadsPerRow : 0));
             break;
         case SPMV_KERNEL_ELL:
             MXS_TRY(run_ell<T>(p->numRows, p->ellWidth, p->ellCol, static_cast<const T*>(p->ellVal), x, y, alpha, beta,
@@ -174,7 +177,13 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
         }
     } else if (v.kernel == SPMV_KERNEL_CSR5 || v.kernel == SPMV_KERNEL_BAND) {
         const int sigma = 32 * v.itemsPerThread;
-        if (v.kernel == SPMV_KERNEL_BAND && !band_shape_supported(v.blockSize, v.itemsPerThread)) {
+        if (v.kernel == SPMV_KERNEL_CSR5 && v.vectorWidth == 32 &&
+            (v.threadsPerRow > 0 ? (v.blockSize != 256 && v.blockSize != 512 && v.blockSize != 1024)
+                                 : (v.blockSize != 128 && v.blockSize != 256 && v.blockSize != 512))) {
+            set_error(__FILE__, __LINE__, "ordered CSR5 needs blockSize 128/256/512 (256/512/1024 persistent), got %d",
+                      v.blockSize);
+            st = SPMV_ERROR_INTERNAL;
+        } else if (v.kernel == SPMV_KERNEL_BAND && !band_shape_supported(v.blockSize, v.itemsPerThread)) {
             set_error(__FILE__, __LINE__, "unsupported band shape block=%d ept=%d", v.blockSize, v.itemsPerThread);
             st = SPMV_ERROR_INTERNAL;
         } else if (sigma != 128 && sigma != 256 && sigma != 512) {
@@ -204,6 +213,9 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
                 e = cudaMemsetAsync(p->errFlag, 0, sizeof(int), h->stream);
                 st = e == cudaSuccess ? csr5_tiles(rowPtr, R, N, sigma, p->csr5TileRow, p->csr5TileOff, h->stream)
                                       : cuda_fail(e, "plan build", __FILE__, __LINE__);
+                long long empties = 1;
+                if (st == SPMV_SUCCESS) st = count_empty_rows(rowPtr, R, &empties, h->stream);
+                p->noEmptyRows = st == SPMV_SUCCESS && empties == 0;
                 if (st == SPMV_SUCCESS) {
                     e = cudaStreamSynchronize(h->stream);
                     if (e != cudaSuccess) st = cuda_fail(e, "plan build", __FILE__, __LINE__);

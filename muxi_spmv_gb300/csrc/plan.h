@@ -27,6 +27,7 @@ struct spmv_plan_s {
     int* csr5CarryRow = nullptr;
     void* csr5CarryVal = nullptr;
     int* errFlag = nullptr;  // device word raised by a pipelined kernel whose wait gave up
+    bool noEmptyRows = false;  // checked at plan creation (CSR5 kernels skip the empty-row pass)
     // ELL: column-major copy of the matrix
     int ellWidth = 0;
     void* ellBuf = nullptr;

@@ -10,6 +10,8 @@ spmv_status_t csr5_tiles(const int* rowPtr, int numRows, int nnz, int sigma, int
                          cudaStream_t s);
 // Host result: the longest row.
 spmv_status_t max_row_length(const int* rowPtr, int numRows, int* out, cudaStream_t s);
+// Number of rows without nonzeros (synchronises the stream).
+spmv_status_t count_empty_rows(const int* rowPtr, int numRows, long long* out, cudaStream_t s);
 template <typename T>
 spmv_status_t csr_to_ell(int numRows, const int* rowPtr, const int* colIdx, const T* values, int width,
                          int* ellCol, T* ellVal, long long* truncated, cudaStream_t s);

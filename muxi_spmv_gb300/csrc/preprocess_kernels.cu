@@ -59,6 +59,38 @@ __global__ void row_lengths_kernel(const int* __restrict__ rowPtr, int numRows, 
     if ((threadIdx.x & 31) == 0 && maxLen) atomicMax(maxLen, l);
 }
 
+__global__ void empty_rows_kernel(const int* __restrict__ rowPtr, int numRows, unsigned long long* __restrict__ out) {
+    unsigned long long n = 0;
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < numRows;
+         r += (long long)gridDim.x * blockDim.x)
+        n += rowPtr[r] == rowPtr[r + 1];
+    for (int off = 16; off > 0; off >>= 1) n += __shfl_xor_sync(kFull, n, off);
+    if ((threadIdx.x & 31) == 0 && n) atomicAdd(out, n);
+}
+
+spmv_status_t count_empty_rows(const int* rowPtr, int numRows, long long* out, cudaStream_t s) {
+    if (!out) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "out is NULL");
+    *out = 0;
+    if (numRows <= 0) return SPMV_SUCCESS;
+    if (!rowPtr) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "rowPtr is NULL");
+    void* buf = nullptr;
+    MXS_TRY(scratch_alloc(&buf, sizeof(unsigned long long), s));
+    unsigned long long* d = static_cast<unsigned long long*>(buf);
+    unsigned long long h = 0;
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof(*d), s);
+    if (e == cudaSuccess) {
+        const unsigned g = grid_for(numRows, 256);
+        empty_rows_kernel<<<g < 4096u ? g : 4096u, 256, 0, s>>>(rowPtr, numRows, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    scratch_free(buf, s);
+    if (e != cudaSuccess) return cuda_fail(e, "empty rows", __FILE__, __LINE__);
+    *out = (long long)h;
+    return SPMV_SUCCESS;
+}
+
 spmv_status_t max_row_length(const int* rowPtr, int numRows, int* out, cudaStream_t s) {
     if (!out) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "out is NULL");
     *out = 0;

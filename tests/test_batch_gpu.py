@@ -149,10 +149,10 @@ def test_uneven_batch_small_sample(mx, cuda, handle):
             assert (np.abs(Y[:, j] - yr) <= 1e-5 * absum).all()
 
 
-@pytest.mark.parametrize("k,variant", [(1, {"nnzPerSlot": 16, "blocksPerSM": 2, "chunkNnz": 1024}),
-                                       (2, {"nnzPerSlot": 16, "blocksPerSM": 3, "chunkNnz": 4096}),
-                                       (1, {"nnzPerSlot": 8, "blocksPerSM": 3, "chunkNnz": 256}),
-                                       (16, {"nnzPerSlot": 8, "blocksPerSM": 3, "chunkNnz": 64})])
+@pytest.mark.parametrize("k,variant", [(1, {"nnzPerSlot": 4, "blocksPerSM": 3, "chunkNnz": 1024}),
+                                       (2, {"nnzPerSlot": 4, "blocksPerSM": 2, "chunkNnz": 4096}),
+                                       (1, {"nnzPerSlot": 8, "blocksPerSM": 2, "chunkNnz": 256}),
+                                       (16, {"nnzPerSlot": 4, "blocksPerSM": 3, "chunkNnz": 32})])
 def test_batch_variants_match_oracle(mx, cuda, handle, hbatch, dmats, k, variant):
     from muxi_spmv_gb300 import batch as B
     rng = np.random.default_rng(100 + k)
@@ -169,6 +169,6 @@ def test_batch_variants_match_oracle(mx, cuda, handle, hbatch, dmats, k, variant
         _check(hbatch, X, Y0, [y.cpu().numpy()[:y0.size] for y, y0 in zip(dY, Y0)], k, 0.75, 0.25)
     plan.destroy()
     with pytest.raises(mx.SpmvError):
-        B.BatchPlan(handle, dmats, 4, {"nnzPerSlot": 16})  # not built for k = 4
+        B.BatchPlan(handle, dmats, 4, {"nnzPerSlot": 8, "blocksPerSM": 3})  # not built
     with pytest.raises(mx.SpmvError):
         B.BatchPlan(handle, dmats, 1, {"chunkNnz": 300})  # not a multiple of the tile

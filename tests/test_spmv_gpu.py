@@ -95,22 +95,26 @@ def test_variants_match_oracle(mx, cuda, cases, var, dtype):
             check(y, y0, A, xh, alpha, beta)
 
 
-PLAN_VARIANTS = [("band", 7, 256, 8), ("band", 7, 256, 4), ("band", 7, 512, 8), ("band", 7, 512, 4),
-                 ("csr5_512", 4, 256, 16), ("csr5_128", 4, 256, 4)]
+PLAN_VARIANTS = [("band", 7, 256, 8, 4, 0), ("band", 7, 256, 4, 4, 0), ("band", 7, 512, 8, 4, 0),
+                 ("band", 7, 512, 4, 4, 0), ("csr5_512", 4, 256, 16, 4, 0), ("csr5_128", 4, 256, 4, 4, 0),
+                 ("csr5o_128", 4, 256, 4, 32, 0), ("csr5o_256", 4, 256, 8, 32, 0), ("csr5o_512", 4, 256, 16, 32, 0),
+                 ("csr5o_b128", 4, 128, 8, 32, 0), ("csr5o_b512", 4, 512, 8, 32, 0),
+                 ("csr5p_256c3", 4, 256, 8, 32, 3), ("csr5p_512c64", 4, 512, 4, 32, 64),
+                 ("csr5p_1024c32", 4, 1024, 8, 32, 32)]
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
-@pytest.mark.parametrize("var", PLAN_VARIANTS, ids=[f"{v[0]}b{v[2]}e{v[3]}" for v in PLAN_VARIANTS])
+@pytest.mark.parametrize("var", PLAN_VARIANTS, ids=[f"{v[0]}b{v[2]}e{v[3]}w{v[4]}" for v in PLAN_VARIANTS])
 def test_plan_variants_match_oracle(mx, cuda, handle, cases, var, dtype):
     """Plan-only kernels (tile metadata built at plan creation): the windowed
     persistent kernel and CSR5 at every tile size, on every edge case."""
     torch = cuda
-    name_, kernel, block, ept = var
+    name_, kernel, block, ept, vw, tpr = var
     for name, (rp, ci, v, cols) in cases.items():
         A = device_csr(mx, rp, ci, v.astype(dtype), cols)
         xh = mx.gen_vector(cols, 77, dtype=dtype)
         x = torch.from_numpy(xh).cuda()
-        p = mx.Plan(handle, A, mx.make_variant(kernel, block, 0, ept, 4))
+        p = mx.Plan(handle, A, mx.make_variant(kernel, block, tpr, ept, vw))
         for alpha, beta in ((1.0, 0.0), (-0.5, 2.0)):
             y0 = mx.gen_vector(A.numRows, 99, dtype=dtype)
             y = torch.from_numpy(y0.copy()).cuda()
