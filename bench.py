@@ -3,8 +3,9 @@
 Default workload: powerlaw8m FP32 -- 8,388,608^2 CSR, Zipf(1.8) row lengths on
 [1,65,536], 70% of columns within +-4,096 of the diagonal, 30% uniform (about
 184M nonzeros, 1.57 GB of algorithmic traffic).  One step = one
-y = A*x through a plan of the C ABI (merge-path tile kernel + carry fix-up),
-inputs resident in HBM.  The matrix (1.5 GB) is larger than the 129 MB L2, so
+y = A*x through a plan of the C ABI (the default AUTO variant: CSR5 tiles of
+256 nonzeros with gathers in nonzero order + carry fix-up), inputs resident in
+HBM.  --workload uneven1024 runs the batched uneven SpMV/SpMM instead.  The matrix (1.5 GB) is larger than the 129 MB L2, so
 no flush is needed between steps.
 
 Algorithmic bytes per SpMV (the roofline numerator):
@@ -266,7 +267,8 @@ def gpu_arm(args):
     value = ws * nbytes / (step_ms * 1e-3) / 1e9
     e2e_val = ws * nbytes / (e2e_ms * 1e-3) / 1e9
     pv = plan.variant.as_dict()
-    kern_names = {mx.KERNEL_MERGE: "merge_vec_kernel", mx.KERNEL_CSR5: "csr5_tile_kernel",
+    kern_names = {mx.KERNEL_MERGE: "merge_vec_kernel",
+                  mx.KERNEL_CSR5: "csr5_ordered_kernel" if pv["vectorWidth"] == 32 else "csr5_tile_kernel",
                   mx.KERNEL_BAND: "band_block_kernel", mx.KERNEL_ELL: "ell_kernel",
                   mx.KERNEL_SCALAR: "csr_rows_kernel", mx.KERNEL_VECTOR: "csr_rows_kernel"}
     # merge-path, CSR5 and band plans launch the tile kernel and a carry fix-up

@@ -50,7 +50,12 @@ csr5_tile_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int
 //     tile's carry.
 //   * Any other tile hands each lane its E consecutive products through
 //     shared memory and runs the CSR5 row logic.
-// sRp / sP: this warp's shared regions (csr5_rp_cap<E>() ints, 32E values).
+// sRp / sP: this warp's shared regions (kOrderedRpCap ints, 32E values).
+// The rowPtr slice holds up to kOrderedRpCap entries (tiles spanning up to
+// 62 rows, nine in ten of the general tiles of a power-law matrix); a tile
+// over more rows reads rowPtr from global memory.  Small slices leave the
+// SM's L1 to the x gathers.
+constexpr int kOrderedRpCap = 64;
 template <typename T, int E>
 struct OrderedLoad {
     int rFirst, rLast;
@@ -107,10 +112,10 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
     }
 
     const int nRp = rLast - rFirst + 2;
-    const bool staged = nRp <= csr5_rp_cap<E>();
+    const bool staged = nRp <= kOrderedRpCap;
     if (staged) {
 #pragma unroll
-        for (int k = 0; k < csr5_rp_per_lane<E>(); ++k) {
+        for (int k = 0; k < kOrderedRpCap / 32; ++k) {
             const int i = lane + 32 * k;
             if (i < nRp) sRp[i] = __ldg(rowPtr + rFirst + i);
         }
@@ -142,8 +147,9 @@ __device__ __forceinline__ void csr5_ordered_tile(long long t, int lane, int num
 }
 
 // One tile per warp, BLOCK threads per block, MINB resident blocks per SM
-// (the launch bound sets the register budget: 128x16 and 512x4 keep 64 warps
-// per SM at 32 registers, 256x6 keeps 48 at 40).
+// (the launch bound sets the register budget: 128x16, 512x4 and 1024x2 keep
+// 64 warps per SM at 32 registers, 256x6 keeps 48 at 40).  Larger blocks put
+// more consecutive tiles on one SM, so their gathers share that SM's L1.
 template <typename T, int E, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB)
 csr5_ordered_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int* __restrict__ colIdx,
@@ -151,7 +157,7 @@ csr5_ordered_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const 
                     int betaZero, const int* __restrict__ tileRow, long long tiles, int* __restrict__ carryRow,
                     T* __restrict__ carryVal, int noEmptyRows) {
     constexpr int WARPS = BLOCK / 32;
-    __shared__ int sRpAll[WARPS][csr5_rp_cap<E>()];
+    __shared__ int sRpAll[WARPS][kOrderedRpCap];
     __shared__ __align__(16) T sPAll[WARPS][32 * E];
     const long long t = ((long long)blockIdx.x * BLOCK + threadIdx.x) >> 5;
     if (t >= tiles) return;  // uniform per warp
@@ -171,7 +177,7 @@ csr5_ordered_persistent_kernel(int numRows, int nnz, const int* __restrict__ row
                                const T* __restrict__ values, const T* __restrict__ x, T* __restrict__ y, T alpha,
                                T beta, int betaZero, const int* __restrict__ tileRow, long long tiles,
                                int* __restrict__ carryRow, T* __restrict__ carryVal, int noEmptyRows, int chunk) {
-    __shared__ int sRpAll[WARPS][csr5_rp_cap<E>()];
+    __shared__ int sRpAll[WARPS][kOrderedRpCap];
     __shared__ __align__(16) T sPAll[WARPS][32 * E];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // Tile and chunk counts fit in int: plans cap nnz below 2^31.
@@ -252,7 +258,8 @@ static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* ca
             case 128: MXS_ORDERED(128, wide ? 6 : 16); break;
             case 256: MXS_ORDERED(256, wide ? 3 : 6); break;
             case 512: MXS_ORDERED(512, wide ? 2 : 4); break;
-            default: MXS_FAIL(SPMV_ERROR_INTERNAL, "ordered CSR5 block must be 128, 256 or 512 (got %d)", block);
+            case 1024: MXS_ORDERED(1024, wide ? 1 : 2); break;
+            default: MXS_FAIL(SPMV_ERROR_INTERNAL, "ordered CSR5 block must be 128, 256, 512 or 1024 (got %d)", block);
         }
 #undef MXS_ORDERED
         return SPMV_SUCCESS;

@@ -98,7 +98,7 @@ def test_variants_match_oracle(mx, cuda, cases, var, dtype):
 PLAN_VARIANTS = [("band", 7, 256, 8, 4, 0), ("band", 7, 256, 4, 4, 0), ("band", 7, 512, 8, 4, 0),
                  ("band", 7, 512, 4, 4, 0), ("csr5_512", 4, 256, 16, 4, 0), ("csr5_128", 4, 256, 4, 4, 0),
                  ("csr5o_128", 4, 256, 4, 32, 0), ("csr5o_256", 4, 256, 8, 32, 0), ("csr5o_512", 4, 256, 16, 32, 0),
-                 ("csr5o_b128", 4, 128, 8, 32, 0), ("csr5o_b512", 4, 512, 8, 32, 0),
+                 ("csr5o_b128", 4, 128, 8, 32, 0), ("csr5o_b512", 4, 512, 8, 32, 0), ("csr5o_b1024", 4, 1024, 8, 32, 0),
                  ("csr5p_256c3", 4, 256, 8, 32, 3), ("csr5p_512c64", 4, 512, 4, 32, 64),
                  ("csr5p_1024c32", 4, 1024, 8, 32, 32)]
 
