@@ -192,10 +192,23 @@ def gpu_arm(args):
     if args.variant:
         k, b, t, i, w = (int(z) for z in args.variant.split(","))
         var = mx.make_variant(k, b, t, i, w)
+    perm = None
+    if args.colperm != "none":
+        # Column reorder on the GPU (reorderColumns / "RCM" / frequency orders),
+        # columns re-sorted within rows; x is permuted to match, y is unchanged.
+        kind = {"com": mx.COLPERM_CENTER_OF_MASS, "minrow": mx.COLPERM_MIN_ROW,
+                "freq": mx.COLPERM_FREQUENCY}[args.colperm]
+        with torch.cuda.stream(stream):
+            perm, _ = mx.column_perm(A, kind, stream)
+            A.d_colIdx[:A.nnz].copy_(mx.apply_column_perm(A, perm, stream))
+            mx.sort_columns_within_rows(A, stream)
+        stream.synchronize()
     plan = mx.Plan(h, A, var)
     distinct = mx.count_distinct_columns(A, stream)
     nbytes = algorithmic_bytes(A.numRows, A.nnz, distinct, vs)
-    x = torch.from_numpy(xh).to(dev)
+    x0 = torch.from_numpy(xh).to(dev)
+    x = mx.permute_x(perm, x0, stream) if perm is not None else x0
+    stream.synchronize()
     y = torch.empty(A.numRows, dtype=tdt, device=dev)
 
     # Parity of the benchmarked matrix (full size) against the FP64 oracle.
@@ -235,20 +248,28 @@ def gpu_arm(args):
     # ---- end to end: host x in, host y out, through the same C-ABI call ----
     x_pin = torch.from_numpy(xh).pin_memory()
     y_pin = torch.empty(A.numRows, dtype=tdt).pin_memory()
+    def e2e_step():
+        if perm is None:
+            x.copy_(x_pin, non_blocking=True)
+        else:  # host x arrives in the original column order
+            x0.copy_(x_pin, non_blocking=True)
+            mx.check(mx.lib().spmv_permute_x_f32(x.numel(), perm.data_ptr(), x0.data_ptr(), x.data_ptr(),
+                                                 stream.cuda_stream) if vs == 4 else
+                     mx.lib().spmv_permute_x_f64(x.numel(), perm.data_ptr(), x0.data_ptr(), x.data_ptr(),
+                                                 stream.cuda_stream), "permute_x")
+        plan.exec(x, y)
+        y_pin.copy_(y, non_blocking=True)
+
     with torch.cuda.stream(stream):
         for _ in range(max(1, args.warmup)):
-            x.copy_(x_pin, non_blocking=True)
-            plan.exec(x, y)
-            y_pin.copy_(y, non_blocking=True)
+            e2e_step()
     stream.synchronize()
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
     with torch.cuda.stream(stream):
         f0.record(stream)
         for _ in range(args.steps):
-            x.copy_(x_pin, non_blocking=True)
-            plan.exec(x, y)
-            y_pin.copy_(y, non_blocking=True)
+            e2e_step()
         f1.record(stream)
     torch.cuda.synchronize(dev)
     e2e_ms = f0.elapsed_time(f1) / args.steps
@@ -276,7 +297,7 @@ def gpu_arm(args):
 
     traffic = None
     tf = ROOT / "profiles" / f"traffic_{args.workload}_{args.dtype}.json"
-    if tf.exists():
+    if tf.exists() and perm is None and not args.scale_rows:
         try:
             traffic = json.loads(tf.read_text()).get("dram_bytes_per_launch")
         except Exception:
@@ -285,7 +306,8 @@ def gpu_arm(args):
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(step_ms, 5), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded generators)",
-            "config": {"workload": args.workload, "rows": A.numRows, "cols": A.numCols, "nnz": A.nnz,
+            "config": {"workload": args.workload + (f"+colperm_{args.colperm}" if perm is not None else ""),
+                       "rows": A.numRows, "cols": A.numCols, "nnz": A.nnz,
                        "distinct_cols": distinct, "algorithmic_bytes": int(nbytes), "variant": pv,
                        "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas{ws}",
                        "gflops": round(2 * A.nnz / (step_ms * 1e-3) / 1e9, 2), "generate_s": round(gen_s, 2)},
@@ -544,6 +566,8 @@ def main():
     ap.add_argument("--variant", default="", help="kernel,block,tpr,ipt,vec (spmv_variant_t)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scale-rows", type=int, default=0, help="same law on this many rows (profiling cases)")
+    ap.add_argument("--colperm", default="none", choices=["none", "com", "minrow", "freq"],
+                    help="reorder columns first (centre of mass, the reference's min-row 'RCM', frequency)")
     ap.add_argument("--k", default="1,2,4,8,16", help="right-hand sides (uneven batch workload)")
     ap.add_argument("--batch-count", type=int, default=1024, help="matrices (uneven batch workload)")
     ap.add_argument("--parity-samples", type=int, default=8, help="matrices checked (uneven batch workload)")

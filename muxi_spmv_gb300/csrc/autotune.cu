@@ -32,9 +32,12 @@ static const spmv_variant_t kSpace[] = {
     {SPMV_KERNEL_MERGE, 256, 0, 8, 4},
     {SPMV_KERNEL_MERGE, 256, 0, 12, 4},
     {SPMV_KERNEL_MERGE, 128, 0, 8, 4},
-    {SPMV_KERNEL_CSR5, 256, 0, 4, 1},
     {SPMV_KERNEL_CSR5, 256, 0, 8, 1},
-    {SPMV_KERNEL_CSR5, 256, 0, 16, 1},
+    {SPMV_KERNEL_CSR5, 128, 0, 8, 32},
+    {SPMV_KERNEL_CSR5, 128, 0, 4, 32},
+    {SPMV_KERNEL_CSR5, 256, 0, 8, 32},
+    {SPMV_KERNEL_CSR5, 128, 0, 16, 32},
+    {SPMV_KERNEL_CSR5, 512, 0, 8, 32},
     {SPMV_KERNEL_BAND, 256, 0, 4, 4},
     {SPMV_KERNEL_BAND, 256, 0, 8, 4},
     {SPMV_KERNEL_BAND, 512, 0, 8, 4},

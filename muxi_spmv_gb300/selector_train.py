@@ -38,7 +38,7 @@ from .api import GenSpec, GEN_BANDED, GEN_BLOCKDIAG, GEN_POISSON_UNIFORM, GEN_ZI
 
 LAWS = ("poisson", "zipf", "banded", "blockdiag")
 HEURISTIC_COL = -1  # last column of the label matrix: the heuristic's variant
-DEFAULT_VARIANT = Variant(api.KERNEL_CSR5, 256, 0, 8, 1)
+DEFAULT_VARIANT = Variant(api.KERNEL_CSR5, 128, 0, 8, 32)  # the AUTO plan without a model
 
 
 def _zipf_clip_for_mean(s: float, target: float, cap: int) -> int:
@@ -75,6 +75,12 @@ def spec_for_seed(seed: int, max_rows: int = 10_000_000, max_nnz: int = 600_000_
         nb = int(rng.integers(8, 257))
         spec = GenSpec(GEN_BLOCKDIAG, R, C, float(nb), m, 0.0, 0.0, gseed)
     return spec, law, m
+
+
+def default_index() -> int:
+    """Index in the variant space of the AUTO plan's variant without a model."""
+    key = lambda v: (v.kernel, v.blockSize, v.threadsPerRow, v.itemsPerThread, v.vectorWidth)
+    return next(i for i, v in enumerate(selector.variant_space()) if key(v) == key(DEFAULT_VARIANT))
 
 
 def heuristic_variant(R: int, N: int) -> Variant:
@@ -218,9 +224,7 @@ def evaluate(model, data, split_name: str = "test") -> dict:
     picks = learned_picks(pred, ms[sel])
     r_learn = regrets(picks, ms[sel])
     r_heur = regrets(None, ms[sel], ms_pick=ms_all[sel, HEURISTIC_COL])
-    space = selector.variant_space()
-    di = next(i for i, v in enumerate(space) if (v.kernel, v.blockSize, v.itemsPerThread) ==
-              (DEFAULT_VARIANT.kernel, DEFAULT_VARIANT.blockSize, DEFAULT_VARIANT.itemsPerThread))
+    di = default_index()
     r_def = regrets(np.full(sel.sum(), di), ms[sel])
     best = np.where(ms[sel] > 0, ms[sel], np.inf).argmin(1)
 

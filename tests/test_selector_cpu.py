@@ -129,7 +129,7 @@ def test_committed_model_beats_non_learned_selection_on_held_out_seeds():
     picks = st.learned_picks(pred, ms)
     r_learn = st.regrets(picks, ms)
     r_heur = st.regrets(None, ms, ms_pick=ms_all[te, -1])
-    r_def = st.regrets(np.full(te.sum(), 16), ms)
+    r_def = st.regrets(np.full(te.sum(), st.default_index()), ms)
     assert r_learn.mean() <= 0.05
     assert r_learn.mean() < r_heur.mean()
     assert r_learn.mean() < r_def.mean()

@@ -181,7 +181,7 @@ def _mlp_problem(cuda, shape, batch, seed):
     return X, T, M, mean, std, d
 
 
-@pytest.mark.parametrize("shape,batch", [((32, 128, 128, 22), 200), ((5, 7, 3, 4), 1), ((32, 17, 9, 22), 33)])
+@pytest.mark.parametrize("shape,batch", [((32, 128, 128, 24), 200), ((5, 7, 3, 4), 1), ((32, 17, 9, 24), 33)])
 def test_mlp_forward_and_gradients_match_fp64(sel, cuda, shape, batch):
     X, T, M, mean, std, (dX, dT, dM) = _mlp_problem(cuda, shape, batch, 11)
     m = sel.MLP(*shape, seed=5)
@@ -206,7 +206,7 @@ def test_mlp_forward_and_gradients_match_fp64(sel, cuda, shape, batch):
 
 
 def test_mlp_adam_matches_fp64(sel, cuda):
-    shape, batch = (32, 64, 48, 22), 96
+    shape, batch = (32, 64, 48, 24), 96
     X, T, M, mean, std, (dX, dT, dM) = _mlp_problem(cuda, shape, batch, 12)
     m = sel.MLP(*shape, seed=6)
     m.set_normalization(mean, std)
@@ -229,11 +229,11 @@ def test_mlp_training_reduces_loss(sel, cuda):
     """A learnable target (a fixed random 2-layer function of the inputs)."""
     rng = np.random.default_rng(3)
     X = rng.normal(0, 1, (512, 32)).astype(np.float32)
-    W = rng.normal(0, 0.3, (32, 22))
+    W = rng.normal(0, 0.3, (32, 24))
     T = np.tanh(X @ W).astype(np.float32)
     M = np.ones_like(T)
     dX, dT, dM = (cuda.from_numpy(a).cuda() for a in (X, T, M))
-    m = sel.MLP(32, 64, 64, 22, seed=1)
+    m = sel.MLP(32, 64, 64, 24, seed=1)
     l0, _ = m.gradients(dX, dT, dM)
     for _ in range(300):
         m.train_step(dX, dT, dM, 3e-3)
@@ -242,12 +242,12 @@ def test_mlp_training_reduces_loss(sel, cuda):
 
 
 def test_mlp_save_load_and_corruption(sel, cuda, tmp_path, mx):
-    m = sel.MLP(32, 16, 8, 22, seed=9)
+    m = sel.MLP(32, 16, 8, 24, seed=9)
     m.set_normalization(np.arange(32, dtype=np.float32), np.full(32, 2.0, np.float32))
     path = tmp_path / "m.mxsmlp"
     m.save(path)
     m2 = sel.MLP.load(path)
-    assert m2.shape == (32, 16, 8, 22)
+    assert m2.shape == (32, 16, 8, 24)
     np.testing.assert_array_equal(m2.get_params(), m.get_params())
     X = cuda.randn(7, 32, device="cuda")
     assert cuda.equal(m.forward(X), m2.forward(X))
@@ -280,29 +280,32 @@ def test_autotune_reports_every_variant(mx, sel, cuda, handle, name):
     rp, ci, v, A = _small(mx, name)
     space = sel.variant_space()
     ms, best = sel.autotune(handle, A, None, repeats=0)
-    assert len(ms) == len(space) == 22
+    assert len(ms) == len(space) == 25
     ok = ms > 0
     assert best == int(np.where(ok, ms, np.inf).argmin())
     maxlen = int(np.diff(rp).max())
     ell_ok = A.numRows * maxlen <= 2 * A.nnz
-    assert bool(ok[21]) == ell_ok
-    assert ok[:21].all()
+    ell = [i for i, v in enumerate(space) if v.kernel == mx.KERNEL_ELL]
+    assert len(ell) == 1 and bool(ok[ell[0]]) == ell_ok
+    assert all(ok[i] for i in range(len(space)) if i not in ell)
 
 
 def test_select_modes(mx, sel, cuda, handle):
     rp, ci, v, A = _small(mx, "powerlaw")
     vh, ih = sel.select(handle, A, sel.SELECT_HEURISTIC)
     assert vh.kernel == mx.KERNEL_SCALAR and ih == 1  # mean row length < 32
-    va, ia = sel.select(handle, A, sel.SELECT_AUTOTUNE)
-    assert 0 <= ia < 22
-    model = sel.MLP(32, 32, 32, 22, seed=2)
-    vl, il = sel.select(handle, A, sel.SELECT_LEARNED, model)
     space = sel.variant_space()
-    assert 0 <= il < 22 and space[il].as_dict() == vl.as_dict()
-    assert il != 21  # ELL does not apply to this matrix
+    n = len(space)
+    ell = next(i for i, v in enumerate(space) if v.kernel == mx.KERNEL_ELL)
+    va, ia = sel.select(handle, A, sel.SELECT_AUTOTUNE)
+    assert 0 <= ia < n
+    model = sel.MLP(32, 32, 32, n, seed=2)
+    vl, il = sel.select(handle, A, sel.SELECT_LEARNED, model)
+    assert 0 <= il < n and space[il].as_dict() == vl.as_dict()
+    assert il != ell  # ELL does not apply to this matrix
     f = sel.matrix_features(A).reshape(1, -1)
     pred = host(model.forward(f))[0]
-    pred[21] = np.inf
+    pred[ell] = np.inf
     assert il == int(pred.argmin())
     vk, ik = sel.select(handle, A, sel.SELECT_LEARNED_TOPK, model, topK=3)
     assert ik in list(np.argsort(pred, kind="stable")[:3])
@@ -315,7 +318,7 @@ def test_select_modes(mx, sel, cuda, handle):
 def test_auto_plan_with_registered_selector(mx, sel, cuda):
     h = mx.spmv_create_handle()
     rp, ci, v, A = _small(mx, "powerlaw")
-    model = sel.MLP(32, 32, 32, 22, seed=4)
+    model = sel.MLP(32, 32, 32, len(sel.variant_space()), seed=4)
     sel.set_selector(h, model)
     vl, il = sel.select(h, A, sel.SELECT_LEARNED, model)
     plan = mx.Plan(h, A)
@@ -338,7 +341,7 @@ DEFAULT_MODEL = Path(__file__).resolve().parents[1] / "muxi_spmv_gb300" / "data"
 @pytest.mark.skipif(not DEFAULT_MODEL.exists(), reason="no trained selector model committed")
 def test_committed_model_selects_and_matches_oracle(mx, sel, cuda, handle):
     model = sel.MLP.load(DEFAULT_MODEL)
-    assert model.shape == (32, 128, 128, 22)
+    assert model.shape == (32, 128, 128, len(sel.variant_space()))
     for name in ("poisson", "powerlaw"):
         rp, ci, v, A = _small(mx, name)
         vl, il = sel.select(handle, A, sel.SELECT_LEARNED, model)
