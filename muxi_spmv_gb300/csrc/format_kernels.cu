@@ -22,6 +22,7 @@
 #include "kernels.h"
 #include "formats.h"
 #include "csr5_tile.cuh"
+#include "sort.h"
 
 namespace mxs {
 
@@ -213,6 +214,111 @@ csr5_ordered_persistent_kernel(int numRows, int nnz, const int* __restrict__ row
     }
 }
 
+// Row still open at the end of each tile (-1 if the tile's last row ends in it).
+__global__ void carry_rows_kernel(const int* __restrict__ rowPtr, int numRows, int nnz, int sigma,
+                                  const int* __restrict__ tileRow, long long tiles, int* __restrict__ carry) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tiles) return;
+    const long long tEnd = (t + 1) * sigma < nnz ? (t + 1) * sigma : nnz;
+    int lo = tileRow[t], hi = t + 1 < tiles ? tileRow[t + 1] : numRows - 1;
+    while (lo < hi) {  // last row with rowPtr <= tEnd - 1: the row holding the tile's last nonzero
+        const int mid = (lo + hi + 1) >> 1;
+        if (rowPtr[mid] <= tEnd - 1) lo = mid;
+        else hi = mid - 1;
+    }
+    carry[t] = rowPtr[lo + 1] > tEnd ? lo : -1;
+}
+
+__global__ void chain_flags_kernel(const int* __restrict__ carry, long long tiles, unsigned* __restrict__ isStart,
+                                   unsigned* __restrict__ isEnd) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tiles) return;
+    const int c = carry[t];
+    isStart[t] = c >= 0 && (t == 0 || carry[t - 1] != c);
+    isEnd[t] = c >= 0 && (t + 1 == tiles || carry[t + 1] != c);
+}
+
+__global__ void chain_compact_kernel(const int* __restrict__ carry, const unsigned* __restrict__ isStart,
+                                     const unsigned* __restrict__ startPos, const unsigned* __restrict__ isEnd,
+                                     const unsigned* __restrict__ endPos, long long tiles, int* __restrict__ start,
+                                     int* __restrict__ end, int* __restrict__ row) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tiles) return;
+    if (isStart[t]) {
+        start[startPos[t]] = (int)t;
+        row[startPos[t]] = carry[t];
+    }
+    if (isEnd[t]) end[endPos[t]] = (int)t;
+}
+
+spmv_status_t csr5_chains(const int* rowPtr, int numRows, int nnz, int sigma, const int* tileRow, long long tiles,
+                          void** buf, Csr5Chains* out, cudaStream_t s) {
+    *buf = nullptr;
+    out->n = 0;
+    if (tiles <= 0) return SPMV_SUCCESS;
+    void* tmp = nullptr;
+    const size_t a = ((sizeof(unsigned) * tiles) + 255) & ~size_t(255);
+    MXS_TRY(scratch_alloc(&tmp, 5 * a + 256, s));
+    char* b = static_cast<char*>(tmp);
+    int* carry = reinterpret_cast<int*>(b);
+    unsigned* isStart = reinterpret_cast<unsigned*>(b + a);
+    unsigned* isEnd = reinterpret_cast<unsigned*>(b + 2 * a);
+    unsigned* startPos = reinterpret_cast<unsigned*>(b + 3 * a);
+    unsigned* endPos = reinterpret_cast<unsigned*>(b + 4 * a);
+    unsigned* total = reinterpret_cast<unsigned*>(b + 5 * a);
+    const unsigned g = grid_for(tiles, 256);
+    carry_rows_kernel<<<g, 256, 0, s>>>(rowPtr, numRows, nnz, sigma, tileRow, tiles, carry);
+    chain_flags_kernel<<<g, 256, 0, s>>>(carry, tiles, isStart, isEnd);
+    spmv_status_t st = cudaGetLastError() == cudaSuccess ? SPMV_SUCCESS : SPMV_ERROR_DEVICE;
+    if (st == SPMV_SUCCESS) st = scan_exclusive_u32(isStart, startPos, tiles, total, s);
+    unsigned n = 0;
+    if (st == SPMV_SUCCESS) st = scan_exclusive_u32(isEnd, endPos, tiles, nullptr, s);
+    if (st == SPMV_SUCCESS) {
+        cudaError_t e = cudaMemcpyAsync(&n, total, sizeof(n), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = cuda_fail(e, "carry chains", __FILE__, __LINE__);
+    }
+    if (st == SPMV_SUCCESS && n > 0) {
+        cudaError_t e = cudaMalloc(buf, 3 * sizeof(int) * (size_t)n);
+        if (e != cudaSuccess) {
+            *buf = nullptr;
+            st = cuda_fail(e, "carry chain table", __FILE__, __LINE__);
+        } else {
+            int* start = static_cast<int*>(*buf);
+            chain_compact_kernel<<<g, 256, 0, s>>>(carry, isStart, startPos, isEnd, endPos, tiles, start, start + n,
+                                                   start + 2 * n);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) st = cuda_fail(e, "carry chains", __FILE__, __LINE__);
+            out->start = start;
+            out->end = start + n;
+            out->row = start + 2 * n;
+        }
+    }
+    scratch_free(tmp, s);
+    if (st != SPMV_SUCCESS) {
+        if (*buf) cudaFree(*buf);
+        *buf = nullptr;
+        out->n = -1;
+        return st;
+    }
+    out->n = n;
+    return SPMV_SUCCESS;
+}
+
+// Adds each chain's carries in tile order.
+template <typename T>
+__global__ void csr5_chain_fixup_kernel(long long chains, const int* __restrict__ start, const int* __restrict__ end,
+                                        const int* __restrict__ row, const T* __restrict__ carryVal, T* __restrict__ y,
+                                        T alpha) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= chains) return;
+    const int e = end[c];
+    T s = T(0);
+    for (int u = start[c]; u <= e; ++u) s += carryVal[u];
+    y[row[c]] += alpha * s;
+}
+
 // Adds each split row's carries in tile order (rows with carry -1 skipped).
 template <typename T>
 __global__ void csr5_fixup_kernel(long long tiles, const int* __restrict__ carryRow, const T* __restrict__ carryVal,
@@ -275,7 +381,7 @@ static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* ca
 template <typename T>
 spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
                        const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain, bool ordered, int block,
-                       int chunk) {
+                       int chunk, const Csr5Chains* chains) {
     if (ordered) {
         if (sigma == 128) MXS_TRY((launch_ordered<T, 4>(tileRow, tiles, carryRow, carryVal, a, block, chunk, s)));
         else if (sigma == 256) MXS_TRY((launch_ordered<T, 8>(tileRow, tiles, carryRow, carryVal, a, block, chunk, s)));
@@ -299,6 +405,14 @@ spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carr
     }
     MXS_LAUNCH_CHECK();
     if (afterMain) MXS_CUDA(cudaEventRecord(afterMain, s));
+    if (chains && chains->n >= 0) {
+        if (chains->n > 0) {
+            csr5_chain_fixup_kernel<T><<<grid_for(chains->n, 256), 256, 0, s>>>(
+                chains->n, chains->start, chains->end, chains->row, carryVal, a.y, a.alpha);
+            MXS_LAUNCH_CHECK();
+        }
+        return SPMV_SUCCESS;
+    }
     return run_csr5_fixup<T>(tiles, carryRow, carryVal, a, s);
 }
 
@@ -314,9 +428,9 @@ template spmv_status_t run_csr5_fixup<float>(long long, const int*, const float*
 template spmv_status_t run_csr5_fixup<double>(long long, const int*, const double*, const RowsArgs<double>&,
                                               cudaStream_t);
 template spmv_status_t run_csr5<float>(int, const int*, long long, int*, float*, const RowsArgs<float>&,
-                                       cudaStream_t, cudaEvent_t, bool, int, int);
+                                       cudaStream_t, cudaEvent_t, bool, int, int, const Csr5Chains*);
 template spmv_status_t run_csr5<double>(int, const int*, long long, int*, double*, const RowsArgs<double>&,
-                                        cudaStream_t, cudaEvent_t, bool, int, int);
+                                        cudaStream_t, cudaEvent_t, bool, int, int, const Csr5Chains*);
 
 // ---------------------------------------------------------------------------
 // ELL

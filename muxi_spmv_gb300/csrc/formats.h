@@ -6,6 +6,22 @@
 
 namespace mxs {
 
+// Carry chains of a CSR5 tiling, built once per matrix: chain c covers tiles
+// start[c]..end[c], all ending inside row row[c], which ends in tile end[c]+1.
+// They depend only on rowPtr and sigma, so a plan precomputes them and its
+// fix-up adds each chain with independent loads.
+struct Csr5Chains {
+    long long n = -1;  // -1: no table (the fix-up walks carryRow instead)
+    const int* start = nullptr;
+    const int* end = nullptr;
+    const int* row = nullptr;
+};
+
+// Builds the chain table for tiles of `sigma` nonzeros.  *buf receives one
+// device allocation (cudaMalloc; the caller frees it) holding the three arrays.
+spmv_status_t csr5_chains(const int* rowPtr, int numRows, int nnz, int sigma, const int* tileRow, long long tiles,
+                          void** buf, Csr5Chains* out, cudaStream_t s);
+
 // Tile kernel then carry fix-up; carryRow/carryVal hold `tiles` entries.
 // ordered: gathers issued in nonzero order (csr5_ordered_kernel); with
 // chunk > 0 the ordered tiles run persistently, blocks of `block` threads
@@ -13,7 +29,7 @@ namespace mxs {
 template <typename T>
 spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
                        const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain = nullptr, bool ordered = false,
-                       int block = 256, int chunk = 0);
+                       int block = 256, int chunk = 0, const Csr5Chains* chains = nullptr);
 
 // Adds the carries of rows split between CSR5 tiles, in tile order.
 template <typename T>

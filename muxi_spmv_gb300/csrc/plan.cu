@@ -92,7 +92,7 @@ static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T
         case SPMV_KERNEL_CSR5:
             MXS_TRY(run_csr5<T>(32 * v.itemsPerThread, p->csr5TileRow, p->csr5Tiles, p->csr5CarryRow,
                                 static_cast<T*>(p->csr5CarryVal), a, s, evEnd, v.vectorWidth == 32, v.blockSize,
-                                v.vectorWidth == 32 ? v.threadsPerRow : 0));
+                                v.vectorWidth == 32 ? v.threadsPerRow : 0, &p->chains));
             break;
         case SPMV_KERNEL_ELL:
             MXS_TRY(run_ell<T>(p->numRows, p->ellWidth, p->ellCol, static_cast<const T*>(p->ellVal), x, y, alpha, beta,
@@ -217,6 +217,8 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
                 long long empties = 1;
                 if (st == SPMV_SUCCESS) st = count_empty_rows(rowPtr, R, &empties, h->stream);
                 p->noEmptyRows = st == SPMV_SUCCESS && empties == 0;
+                if (st == SPMV_SUCCESS && v.kernel == SPMV_KERNEL_CSR5)
+                    st = csr5_chains(rowPtr, R, N, sigma, p->csr5TileRow, T, &p->chainBuf, &p->chains, h->stream);
                 if (st == SPMV_SUCCESS) {
                     e = cudaStreamSynchronize(h->stream);
                     if (e != cudaSuccess) st = cuda_fail(e, "plan build", __FILE__, __LINE__);
@@ -265,6 +267,7 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
     if (st != SPMV_SUCCESS) {
         if (p->mergeBuf) cudaFree(p->mergeBuf);
         if (p->csr5Buf) cudaFree(p->csr5Buf);
+        if (p->chainBuf) cudaFree(p->chainBuf);
         if (p->ellBuf) cudaFree(p->ellBuf);
         delete p;
         return st;
@@ -321,6 +324,7 @@ spmv_status_t spmv_plan_destroy(spmv_plan_t p) {
     }
     if (p->mergeBuf) cudaFree(p->mergeBuf);
     if (p->csr5Buf) cudaFree(p->csr5Buf);
+    if (p->chainBuf) cudaFree(p->chainBuf);
     if (p->ellBuf) cudaFree(p->ellBuf);
     delete p;
     return SPMV_SUCCESS;

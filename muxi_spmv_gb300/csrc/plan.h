@@ -6,6 +6,7 @@
 
 #include "internal.h"
 #include "kernels.h"
+#include "formats.h"
 
 struct spmv_plan_s {
     spmv_type_t type = SPMV_TYPE_FLOAT;
@@ -28,6 +29,8 @@ struct spmv_plan_s {
     void* csr5CarryVal = nullptr;
     int* errFlag = nullptr;  // device word raised by a pipelined kernel whose wait gave up
     bool noEmptyRows = false;  // checked at plan creation (CSR5 kernels skip the empty-row pass)
+    void* chainBuf = nullptr;  // CSR5 carry chains (start / end / row), see Csr5Chains
+    mxs::Csr5Chains chains{};
     // ELL: column-major copy of the matrix
     int ellWidth = 0;
     void* ellBuf = nullptr;
