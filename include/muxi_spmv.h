@@ -157,6 +157,21 @@ SPMV_API spmv_status_t spmv_csr_f64(int numRows, int numCols, int nnz,
                            const double* x, double* y, double alpha, double beta,
                            const spmv_opts_t* opts);
 
+/* opts->operation == SPMV_OP_TRANSPOSE computes y = alpha*A^T*x + beta*y
+ * (x: numRows entries, y: numCols entries) by building A^T in stream-ordered
+ * scratch (spmv_csr_transpose_*) and running it as a normal SpMV; the
+ * reference declares spmv_exec_transpose (spmv_api.h:70-78) without a
+ * definition and scatters with float atomics in its transpose kernel. */
+
+/* CSR of A^T on the device: tRowPtr[numCols+1], tColIdx/tValues[nnz]; row c
+ * of A^T lists the rows of A holding column c in ascending order. */
+SPMV_API spmv_status_t spmv_csr_transpose_f32(int numRows, int numCols, int nnz, const int* rowPtr,
+                                              const int* colIdx, const float* values, int* tRowPtr, int* tColIdx,
+                                              float* tValues, cudaStream_t stream);
+SPMV_API spmv_status_t spmv_csr_transpose_f64(int numRows, int numCols, int nnz, const int* rowPtr,
+                                              const int* colIdx, const double* values, int* tRowPtr, int* tColIdx,
+                                              double* tValues, cudaStream_t stream);
+
 /* FP32 CSR SpMV that allocates no device memory (no counterpart in the
  * reference).  Same kernels and results as spmv_csr_f32 (default merge-path
  * variant), for callers that cannot allocate: code recording a CUDA graph,
@@ -469,6 +484,44 @@ SPMV_API spmv_status_t spmv_gen_device_fill_f32(const spmv_gen_params_t* p, cons
                                                 float* values, cudaStream_t stream);
 SPMV_API spmv_status_t spmv_gen_device_vector_f32(long long n, unsigned long long seed, double lo, double hi,
                                                   float* out, cudaStream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Matrix Market files <-> host CSR (src/generators/mtx_io.h:22-85).     */
+/* The reader follows readMTXFile (mtx_io.cu:111-222): 1-based entries,  */
+/* pattern -> 1, symmetric files mirrored unless expandSymmetric is 0,   */
+/* entries sorted by (row, column), duplicates kept in file order.       */
+/* Complex files are refused; skew-symmetric mirrors are negated.  The   */
+/* writer emits a banner the reader accepts and exact values.            */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    int isSymmetric;
+    int isSkew;
+    int isComplex;
+    int isPattern;
+    int isInteger;
+    int numRows;
+    int numCols;
+    int nnz;          /* entries stored in the file */
+} spmv_mtx_header_t;
+
+/* Host CSR owned by the library after spmv_mtx_read (free with
+ * spmv_host_csr_free); values are float or double per `type`. */
+typedef struct {
+    int numRows;
+    int numCols;
+    int nnz;
+    int* rowPtr;
+    int* colIdx;
+    void* values;
+    spmv_type_t type;
+} spmv_host_csr_t;
+
+SPMV_API spmv_status_t spmv_mtx_read_header(const char* path, spmv_mtx_header_t* header);
+SPMV_API spmv_status_t spmv_mtx_read(const char* path, spmv_type_t type, int expandSymmetric, spmv_host_csr_t* out);
+/* writeSymmetric: write the upper triangle (column >= row) only, as the
+ * reference's writer does (mtx_io.cu:245-262). */
+SPMV_API spmv_status_t spmv_mtx_write(const char* path, const spmv_host_csr_t* m, int writeSymmetric);
+SPMV_API void spmv_host_csr_free(spmv_host_csr_t* m);
 
 /* ------------------------------------------------------------------ */
 /* Kernel selection.  The reference selects by a fixed rule on the     */

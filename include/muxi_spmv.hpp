@@ -43,6 +43,9 @@ namespace detail {
 template <typename T> struct is_supported : std::integral_constant<bool, std::is_same<T, float>::value ||
                                                                          std::is_same<T, double>::value> {};
 inline cudaStream_t stream_of(const spmv_opts_t& o) { return reinterpret_cast<cudaStream_t>(o.stream); }
+template <typename T> constexpr spmv_type_t type_of() {
+    return std::is_same<T, float>::value ? SPMV_TYPE_FLOAT : SPMV_TYPE_DOUBLE;
+}
 }  // namespace detail
 
 // ---------------------------------------------------------------------------
@@ -329,13 +332,26 @@ spmv_status_t spmv_exec(spmv_handle_t* handle, spmv_format_t format, const void*
     }
 }
 
-// spmv_exec_transpose<T> (spmv_api.h:70-78): not provided by this library
-// yet; returns SPMV_ERROR_UNSUPPORTED_FORMAT (the reference declares it
-// without defining it).
+// spmv_exec_transpose<T> (spmv_api.h:70-78, declared there without a
+// definition): y = alpha*A^T*x + beta*y for CSR matrices (x: numRows
+// entries, y: numCols), on the handle's stream; other formats are refused.
 template <typename FloatType>
-spmv_status_t spmv_exec_transpose(spmv_handle_t*, spmv_format_t, const void*, const FloatType*, FloatType*,
-                                  FloatType = 1.0, FloatType = 0.0) {
-    return SPMV_ERROR_UNSUPPORTED_FORMAT;
+spmv_status_t spmv_exec_transpose(spmv_handle_t* handle, spmv_format_t format, const void* matrix,
+                                  const FloatType* x, FloatType* y, FloatType alpha = 1.0, FloatType beta = 0.0) {
+    static_assert(detail::is_supported<FloatType>::value, "float or double");
+    if (!handle) return SPMV_ERROR_INVALID_HANDLE;
+    if (format != SPMV_FORMAT_CSR) return SPMV_ERROR_UNSUPPORTED_FORMAT;
+    const CSRMatrix<FloatType>& A = *static_cast<const CSRMatrix<FloatType>*>(matrix);
+    spmv_opts_t o = handle->opts;
+    o.operation = SPMV_OP_TRANSPOSE;
+    o.stream = (void*)handle->stream;
+    if (std::is_same<FloatType, float>::value)
+        return spmv_csr_f32(A.numRows, A.numCols, A.nnz, A.d_rowPtr, A.d_colIdx,
+                            reinterpret_cast<const float*>(A.d_values), reinterpret_cast<const float*>(x),
+                            reinterpret_cast<float*>(y), (float)alpha, (float)beta, &o);
+    return spmv_csr_f64(A.numRows, A.numCols, A.nnz, A.d_rowPtr, A.d_colIdx, reinterpret_cast<const double*>(A.d_values),
+                        reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y), (double)alpha, (double)beta,
+                        &o);
 }
 
 // ---------------------------------------------------------------------------
@@ -424,6 +440,58 @@ spmv_status_t sortColumnsWithinRows(CSRMatrix<FloatType>& matrix) {
     cudaFree(dVal);
     return st;
 }
+
+// Matrix Market I/O: src/generators/mtx_io.h:22-85 (namespace muxi_spmv::io).
+namespace io {
+
+struct MTXHeader {
+    bool isSymmetric;
+    bool isComplex;
+    bool isPattern;
+    bool isInteger;
+    int numRows;
+    int numCols;
+    int nnz;
+};
+
+inline spmv_status_t readMTXHeader(const char* filename, MTXHeader& header) {
+    spmv_mtx_header_t h;
+    const spmv_status_t st = spmv_mtx_read_header(filename, &h);
+    if (st != SPMV_SUCCESS) return st;
+    header = MTXHeader{h.isSymmetric != 0, h.isComplex != 0, h.isPattern != 0, h.isInteger != 0, h.numRows,
+                       h.numCols, h.nnz};
+    return SPMV_SUCCESS;
+}
+
+// Fills the host arrays of `matrix` (it takes ownership of them).
+template <typename FloatType>
+spmv_status_t readMTXFile(const char* filename, CSRMatrix<FloatType>& matrix, bool expandSymmetric = true) {
+    spmv_host_csr_t h;
+    const spmv_status_t st = spmv_mtx_read(filename, detail::type_of<FloatType>(), expandSymmetric ? 1 : 0, &h);
+    if (st != SPMV_SUCCESS) return st;
+    if (matrix.ownsHostMemory) {
+        std::free(matrix.rowPtr);
+        std::free(matrix.colIdx);
+        std::free(matrix.values);
+    }
+    matrix.numRows = h.numRows;
+    matrix.numCols = h.numCols;
+    matrix.nnz = h.nnz;
+    matrix.rowPtr = h.rowPtr;
+    matrix.colIdx = h.colIdx;
+    matrix.values = static_cast<FloatType*>(h.values);
+    matrix.ownsHostMemory = true;
+    return SPMV_SUCCESS;
+}
+
+template <typename FloatType>
+spmv_status_t writeMTXFile(const char* filename, const CSRMatrix<FloatType>& matrix, bool writeSymmetric = false) {
+    spmv_host_csr_t h{matrix.numRows, matrix.numCols, matrix.nnz, matrix.rowPtr, matrix.colIdx,
+                      static_cast<void*>(matrix.values), detail::type_of<FloatType>()};
+    return spmv_mtx_write(filename, &h, writeSymmetric ? 1 : 0);
+}
+
+}  // namespace io
 
 }  // namespace muxi_spmv
 

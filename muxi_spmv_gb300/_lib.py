@@ -72,6 +72,18 @@ class BatchMatrix(C.Structure):
                 ("colIdx", C.c_void_p), ("values", C.c_void_p)]
 
 
+class MtxHeader(C.Structure):
+    """spmv_mtx_header_t."""
+    _fields_ = [("isSymmetric", C.c_int), ("isSkew", C.c_int), ("isComplex", C.c_int), ("isPattern", C.c_int),
+                ("isInteger", C.c_int), ("numRows", C.c_int), ("numCols", C.c_int), ("nnz", C.c_int)]
+
+
+class HostCSR(C.Structure):
+    """spmv_host_csr_t."""
+    _fields_ = [("numRows", C.c_int), ("numCols", C.c_int), ("nnz", C.c_int), ("rowPtr", C.POINTER(C.c_int)),
+                ("colIdx", C.POINTER(C.c_int)), ("values", C.c_void_p), ("type", C.c_int)]
+
+
 class BatchVariant(C.Structure):
     """spmv_batch_variant_t."""
     _fields_ = [("nnzPerSlot", C.c_int), ("blocksPerSM", C.c_int), ("chunkNnz", C.c_int)]
@@ -160,6 +172,12 @@ SIGNATURES = {
     "spmv_mlp_load": (S, [C.c_char_p, C.POINTER(P)]),
     "spmv_select": (S, [C.POINTER(Handle), I, P, I, I, I, I, I, P, P, P, C.POINTER(Variant), C.POINTER(C.c_int)]),
     "spmv_set_selector": (S, [C.POINTER(Handle), P]),
+    "spmv_csr_transpose_f32": (S, [I, I, I, P, P, P, P, P, P, P]),
+    "spmv_csr_transpose_f64": (S, [I, I, I, P, P, P, P, P, P, P]),
+    "spmv_mtx_read_header": (S, [C.c_char_p, C.POINTER(MtxHeader)]),
+    "spmv_mtx_read": (S, [C.c_char_p, I, I, C.POINTER(HostCSR)]),
+    "spmv_mtx_write": (S, [C.c_char_p, C.POINTER(HostCSR), I]),
+    "spmv_host_csr_free": (None, [C.POINTER(HostCSR)]),
     "spmv_batch_create": (S, [C.POINTER(Handle), I, C.POINTER(BatchMatrix), I, C.POINTER(P)]),
     "spmv_batch_create_ex": (S, [C.POINTER(Handle), I, C.POINTER(BatchMatrix), I, C.POINTER(BatchVariant),
                                  C.POINTER(P)]),

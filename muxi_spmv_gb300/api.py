@@ -154,6 +154,30 @@ def spmv_csr(A: CSRMatrix, x, y, alpha=1.0, beta=0.0, opts: Opts | None = None):
     return y
 
 
+def spmv_csr_transpose(A: CSRMatrix, x, y, alpha=1.0, beta=0.0, stream=None):
+    """y = alpha*A^T*x + beta*y (the reference's spmv_exec_transpose, spmv_api.h:70-78)."""
+    o = spmv_default_opts(stream)
+    o.operation = _lib.SPMV_OP_TRANSPOSE
+    f = lib().spmv_csr_f32 if _is_f32(A) else lib().spmv_csr_f64
+    check(f(*A.device_args(), _ptr(x), _ptr(y), alpha, beta, C.byref(o)), "spmv_csr (transpose)")
+    return y
+
+
+def csr_transpose(A: CSRMatrix, stream=None) -> CSRMatrix:
+    """CSR of A^T built on the device (host arrays left empty)."""
+    torch = _torch()
+    tdt = torch.float32 if _is_f32(A) else torch.float64
+    B = CSRMatrix(np.zeros(A.numCols + 1, np.int32), np.zeros(0, np.int32), np.zeros(0, A.dtype), A.numRows)
+    B.nnz = A.nnz
+    B.d_rowPtr = torch.empty(A.numCols + 1, dtype=torch.int32, device="cuda")
+    B.d_colIdx = torch.empty(max(A.nnz, 1), dtype=torch.int32, device="cuda")
+    B.d_values = torch.empty(max(A.nnz, 1), dtype=tdt, device="cuda")
+    f = lib().spmv_csr_transpose_f32 if _is_f32(A) else lib().spmv_csr_transpose_f64
+    check(f(*A.device_args(), _ptr(B.d_rowPtr), _ptr(B.d_colIdx), _ptr(B.d_values), _stream_ptr(stream)),
+          "spmv_csr_transpose")
+    return B
+
+
 def make_variant(kernel: int, blockSize: int = 256, threadsPerRow: int = 0, itemsPerThread: int = 0,
                  vectorWidth: int = 1) -> Variant:
     return Variant(kernel, blockSize, threadsPerRow, itemsPerThread, vectorWidth)
@@ -406,6 +430,41 @@ def validate_csr(A: CSRMatrix, stream=None) -> int:
     check(lib().spmv_validate_csr(A.numRows, A.numCols, A.nnz, _ptr(A.d_rowPtr), _ptr(A.d_colIdx), C.byref(b),
                                   _stream_ptr(stream)), "spmv_validate_csr")
     return b.value
+
+
+# ---------------------------------------------------------------------------
+# Matrix Market I/O (src/generators/mtx_io.h:22-85)
+# ---------------------------------------------------------------------------
+def readMTXHeader(filename) -> dict:
+    h = _lib.MtxHeader()
+    check(lib().spmv_mtx_read_header(str(filename).encode(), C.byref(h)), "spmv_mtx_read_header")
+    return {k: getattr(h, k) for k, _ in h._fields_}
+
+
+def readMTXFile(filename, dtype=np.float32, expandSymmetric: bool = True) -> CSRMatrix:
+    """readMTXFile<T> (mtx_io.cu:111-222) -> CSRMatrix with host arrays."""
+    h = _lib.HostCSR()
+    t = SPMV_TYPE_FLOAT if np.dtype(dtype) == np.float32 else SPMV_TYPE_DOUBLE
+    check(lib().spmv_mtx_read(str(filename).encode(), t, 1 if expandSymmetric else 0, C.byref(h)), "spmv_mtx_read")
+    try:
+        rp = np.ctypeslib.as_array(h.rowPtr, shape=(h.numRows + 1,)).copy()
+        ci = np.ctypeslib.as_array(h.colIdx, shape=(max(h.nnz, 1),))[:h.nnz].copy()
+        vt = C.c_float if t == SPMV_TYPE_FLOAT else C.c_double
+        va = np.ctypeslib.as_array(C.cast(h.values, C.POINTER(vt)), shape=(max(h.nnz, 1),))[:h.nnz].copy()
+    finally:
+        lib().spmv_host_csr_free(C.byref(h))
+    return CSRMatrix(rp, ci, va, h.numCols)
+
+
+def writeMTXFile(filename, A: CSRMatrix, writeSymmetric: bool = False):
+    """writeMTXFile<T> (mtx_io.cu:224-271), banner fixed, exact values."""
+    rp = np.ascontiguousarray(A.rowPtr, np.int32)
+    ci = np.ascontiguousarray(A.colIdx, np.int32)
+    va = np.ascontiguousarray(A.values)
+    h = _lib.HostCSR(A.numRows, A.numCols, A.nnz, rp.ctypes.data_as(C.POINTER(C.c_int)),
+                     ci.ctypes.data_as(C.POINTER(C.c_int)), va.ctypes.data_as(C.c_void_p),
+                     SPMV_TYPE_FLOAT if va.dtype == np.float32 else SPMV_TYPE_DOUBLE)
+    check(lib().spmv_mtx_write(str(filename).encode(), C.byref(h), 1 if writeSymmetric else 0), "spmv_mtx_write")
 
 
 # ---------------------------------------------------------------------------

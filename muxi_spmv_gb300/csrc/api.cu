@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "preprocess.h"
 #include "kernels.h"
 #include "plan.h"
 
@@ -150,10 +151,49 @@ static spmv_status_t finish(const spmv_opts_t* opts, cudaStream_t s) {
 template <typename T>
 static spmv_status_t csr_exec(const spmv_variant_t* v, int R, int C, int N, const int* rowPtr,
                               const int* colIdx, const T* values, const T* x, T* y, T alpha, T beta,
+                              const spmv_opts_t* opts);
+
+// y = alpha*A^T*x + beta*y (x has R entries, y has C): the transpose is built
+// in stream-ordered scratch (csr_transpose) and run as a normal CSR SpMV, so
+// the result is deterministic (the reference scattered with float atomics,
+// spmv_csr.cuh:105-107).
+template <typename T>
+static spmv_status_t csr_exec_transpose(const spmv_variant_t* v, int R, int C, int N, const int* rowPtr,
+                                        const int* colIdx, const T* values, const T* x, T* y, T alpha, T beta,
+                                        const spmv_opts_t* opts) {
+    if (R < 0 || C < 0 || N < 0) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "negative dimension (R=%d C=%d nnz=%d)", R, C, N);
+    if (R > 0 && !rowPtr) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "rowPtr is NULL");
+    if (N > 0 && (!colIdx || !values)) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "colIdx/values is NULL");
+    if (C > 0 && !y) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "y (numCols entries) is NULL");
+    if (N > 0 && !x) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "x (numRows entries) is NULL");
+    const cudaStream_t s = opts_stream(opts);
+    if (C == 0) return SPMV_SUCCESS;
+    const size_t a = (sizeof(int) * ((size_t)C + 1) + 255) & ~size_t(255);
+    const size_t b = (sizeof(int) * (size_t)(N > 0 ? N : 1) + 255) & ~size_t(255);
+    void* buf = nullptr;
+    MXS_TRY(scratch_alloc(&buf, a + b + sizeof(T) * (size_t)(N > 0 ? N : 1), s));
+    int* tRp = static_cast<int*>(buf);
+    int* tCi = reinterpret_cast<int*>(static_cast<char*>(buf) + a);
+    T* tVa = reinterpret_cast<T*>(static_cast<char*>(buf) + a + b);
+    spmv_status_t st = csr_transpose<T>(R, C, N, rowPtr, colIdx, values, tRp, tCi, tVa, s);
+    if (st == SPMV_SUCCESS) {
+        spmv_opts_t o = opts ? *opts : spmv_default_opts();
+        o.operation = SPMV_OP_NORMAL;
+        st = csr_exec<T>(v, C, R, N, tRp, tCi, tVa, x, y, alpha, beta, &o);
+    }
+    scratch_free(buf, s);
+    return st;
+}
+
+template <typename T>
+static spmv_status_t csr_exec(const spmv_variant_t* v, int R, int C, int N, const int* rowPtr,
+                              const int* colIdx, const T* values, const T* x, T* y, T alpha, T beta,
                               const spmv_opts_t* opts) {
     clear_error();
+    if (opts && opts->operation == SPMV_OP_TRANSPOSE)
+        return csr_exec_transpose<T>(v, R, C, N, rowPtr, colIdx, values, x, y, alpha, beta, opts);
     if (opts && opts->operation != SPMV_OP_NORMAL)
-        MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "only SPMV_OP_NORMAL is supported by spmv_csr");
+        MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "SPMV_OP_CONJUGATE is not supported (real types only)");
     MXS_TRY(check_csr_args<T>(R, C, N, rowPtr, colIdx, values, x, y));
     const cudaStream_t s = opts_stream(opts);
     if (R == 0) return SPMV_SUCCESS;

@@ -164,4 +164,16 @@ spmv_status_t spmv_sort_columns_within_rows_f64(int R, int C, int N, const int* 
     return sort_within_rows<double>(R, C, N, rowPtr, colIdx, values, stream);
 }
 
+spmv_status_t spmv_csr_transpose_f32(int R, int C, int N, const int* rowPtr, const int* colIdx, const float* values,
+                                     int* tRowPtr, int* tColIdx, float* tValues, cudaStream_t stream) {
+    clear_error();
+    return csr_transpose<float>(R, C, N, rowPtr, colIdx, values, tRowPtr, tColIdx, tValues, stream);
+}
+
+spmv_status_t spmv_csr_transpose_f64(int R, int C, int N, const int* rowPtr, const int* colIdx, const double* values,
+                                     int* tRowPtr, int* tColIdx, double* tValues, cudaStream_t stream) {
+    clear_error();
+    return csr_transpose<double>(R, C, N, rowPtr, colIdx, values, tRowPtr, tColIdx, tValues, stream);
+}
+
 }  // extern "C"

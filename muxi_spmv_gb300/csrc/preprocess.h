@@ -30,5 +30,10 @@ spmv_status_t permute_x(int numCols, const int* perm, const T* x, T* xr, cudaStr
 template <typename T>
 spmv_status_t sort_within_rows(int numRows, int numCols, int nnz, const int* rowPtr, int* colIdx, T* values,
                                cudaStream_t s);
+// CSR of the transpose: tRowPtr[numCols+1], tColIdx/tValues[nnz].  Rows of the
+// transpose list the original rows in ascending order (stable by position).
+template <typename T>
+spmv_status_t csr_transpose(int numRows, int numCols, int nnz, const int* rowPtr, const int* colIdx, const T* values,
+                            int* tRowPtr, int* tColIdx, T* tValues, cudaStream_t s);
 
 }  // namespace mxs

@@ -512,3 +512,70 @@ template spmv_status_t sort_within_rows<float>(int, int, int, const int*, int*, 
 template spmv_status_t sort_within_rows<double>(int, int, int, const int*, int*, double*, cudaStream_t);
 
 }  // namespace mxs
+
+namespace mxs {
+
+// ---------------------------------------------------------------------------
+// Transpose: stable radix sort of the nonzeros by column (ties keep row
+// order), counts of each column scanned into the new row pointers, and a
+// gather of rows and values in sorted order.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void transpose_gather_kernel(long long n, const unsigned* __restrict__ pos,
+                                        const unsigned* __restrict__ rowOf, const T* __restrict__ values,
+                                        int* __restrict__ tCol, T* __restrict__ tVal) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const unsigned p = pos[k];
+    tCol[k] = (int)rowOf[p];
+    tVal[k] = values[p];
+}
+
+template <typename T>
+spmv_status_t csr_transpose(int numRows, int numCols, int nnz, const int* rowPtr, const int* colIdx, const T* values,
+                            int* tRowPtr, int* tColIdx, T* tValues, cudaStream_t s) {
+    if (numRows < 0 || numCols < 0 || nnz < 0) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "negative dimension");
+    if (!tRowPtr) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "tRowPtr is NULL");
+    if (nnz == 0) {
+        MXS_CUDA(cudaMemsetAsync(tRowPtr, 0, sizeof(int) * ((size_t)numCols + 1), s));
+        return SPMV_SUCCESS;
+    }
+    if (!rowPtr || !colIdx || !values || !tColIdx || !tValues) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "NULL array");
+    const size_t n = (size_t)nnz;
+    const size_t a = (sizeof(unsigned) * n + 255) & ~size_t(255);
+    const size_t ac = (sizeof(unsigned) * ((size_t)numCols + 1) + 255) & ~size_t(255);
+    void* buf = nullptr;
+    MXS_TRY(scratch_alloc(&buf, 3 * a + ac, s));
+    char* b = static_cast<char*>(buf);
+    unsigned* keys = reinterpret_cast<unsigned*>(b);
+    unsigned* pos = reinterpret_cast<unsigned*>(b + a);
+    unsigned* rowOf = reinterpret_cast<unsigned*>(b + 2 * a);
+    unsigned* cnt = reinterpret_cast<unsigned*>(b + 3 * a);
+    const unsigned g = grid_for(nnz, 256);
+    cudaError_t e = cudaMemcpyAsync(keys, colIdx, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(unsigned) * ((size_t)numCols + 1), s);
+    spmv_status_t st = e == cudaSuccess ? SPMV_SUCCESS : cuda_fail(e, "transpose", __FILE__, __LINE__);
+    if (st == SPMV_SUCCESS) {
+        iota_kernel<<<g, 256, 0, s>>>(pos, nnz);
+        count_cols_kernel<<<g < 4096u ? g : 4096u, 256, 0, s>>>(nnz, colIdx, cnt);
+        expand_rows_kernel<<<grid_for((long long)numRows * 32, 256), 256, 0, s>>>(rowPtr, numRows, rowOf);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) st = cuda_fail(e, "transpose", __FILE__, __LINE__);
+    }
+    if (st == SPMV_SUCCESS) st = radix_sort_pairs(keys, pos, nnz, bits_for(numCols > 0 ? numCols - 1 : 0), s);
+    if (st == SPMV_SUCCESS)
+        st = scan_exclusive_u32(cnt, reinterpret_cast<unsigned*>(tRowPtr), numCols + 1, nullptr, s);
+    if (st == SPMV_SUCCESS) {
+        transpose_gather_kernel<T><<<g, 256, 0, s>>>(nnz, pos, rowOf, values, tColIdx, tValues);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) st = cuda_fail(e, "transpose", __FILE__, __LINE__);
+    }
+    scratch_free(buf, s);
+    return st;
+}
+template spmv_status_t csr_transpose<float>(int, int, int, const int*, const int*, const float*, int*, int*, float*,
+                                            cudaStream_t);
+template spmv_status_t csr_transpose<double>(int, int, int, const int*, const int*, const double*, int*, int*,
+                                             double*, cudaStream_t);
+
+}  // namespace mxs

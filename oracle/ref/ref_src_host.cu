@@ -3,6 +3,7 @@
 //   src/preprocessing/column_reorder.cuh  reorderColumns (:42-141),
 //                                         sortColumnsWithinRows (:175-201)
 //   src/spmv/ellpack/spmv_ellpack.cu      csr_to_ellpack (:11-70)
+//   src/generators/mtx_io.cu              readMTXFile (:111-222)
 // csr_to_ellpack finishes with cudaMalloc/cudaMemcpy into device arrays; the
 // recipe links this unit against ref_host_cudart.cpp, whose cudaMalloc and
 // cudaMemcpy work on host memory, so the converted arrays can be read back
@@ -10,6 +11,7 @@
 #include <vector>
 #include "preprocessing/column_reorder.cuh"
 #include "spmv/ellpack/spmv_ellpack.cu"
+#include "generators/mtx_io.cu"
 
 using namespace muxi_spmv;
 
@@ -62,4 +64,24 @@ extern "C" int ref_csr_to_ell(int rows, int cols, int nnz, const int* rp, const 
     free(e.d_colIdx);
     free(e.d_values);
     return e.numElements;
+}
+
+// readMTXFile into a reference CSRMatrix; with out arrays NULL only the sizes
+// are returned (rows, cols, nnz), else the CSR is copied out.  Returns the
+// reference's status.
+extern "C" int ref_mtx_read_f64(const char* path, int expand, int* dims, int* rp, int* ci, double* v) {
+    CSRMatrix<double> m;
+    const int st = (int)io::readMTXFile<double>(path, m, expand != 0);
+    if (st != 0) return st;
+    dims[0] = m.numRows;
+    dims[1] = m.numCols;
+    dims[2] = m.nnz;
+    if (rp) {
+        for (int r = 0; r <= m.numRows; ++r) rp[r] = m.rowPtr[r];
+        for (int j = 0; j < m.nnz; ++j) {
+            ci[j] = m.colIdx[j];
+            v[j] = m.values[j];
+        }
+    }
+    return 0;
 }

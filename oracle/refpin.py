@@ -35,11 +35,12 @@ def lib():
             "ref_center_of_mass_perm": [I, I, I, P, P, P, P],
             "ref_sort_within_rows": [I, I, I, P, P, P],
             "ref_csr_to_ell": [I, I, I, P, P, P, I, P, P],
+            "ref_mtx_read_f64": [C.c_char_p, I, P, P, P, P],
         }
         for n, a in sig.items():
             f = getattr(L, n)
             f.argtypes = a
-            f.restype = I if n == "ref_csr_to_ell" else None
+            f.restype = I if n in ("ref_csr_to_ell", "ref_mtx_read_f64") else None
         _lib = L
     return _lib
 
@@ -133,3 +134,18 @@ def csr_to_ell(rowPtr, colIdx, values, cols, maxElements=0):
     ev = np.empty(max(rows * W, 1), np.float32)
     w = lib().ref_csr_to_ell(rows, cols, len(colIdx), _p(rowPtr), _p(colIdx), _p(values), maxElements, _p(ec), _p(ev))
     return ec[: rows * w], ev[: rows * w], w
+
+
+def mtx_read(path, expand=True):
+    """The reference's readMTXFile<double> (src/generators/mtx_io.cu:111-222):
+    (status, rowPtr, colIdx, values, numCols)."""
+    dims = np.zeros(3, np.int32)
+    st = lib().ref_mtx_read_f64(str(path).encode(), 1 if expand else 0, _p(dims), None, None, None)
+    if st != 0:
+        return st, None, None, None, 0
+    rows, cols, nnz = (int(d) for d in dims)
+    rp = np.empty(rows + 1, np.int32)
+    ci = np.empty(max(nnz, 1), np.int32)
+    v = np.empty(max(nnz, 1), np.float64)
+    lib().ref_mtx_read_f64(str(path).encode(), 1 if expand else 0, _p(dims), _p(rp), _p(ci), _p(v))
+    return 0, rp, ci[:nnz], v[:nnz], cols

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <unistd.h>
 #include <vector>
 
 #include "muxi_spmv.hpp"
@@ -151,6 +152,22 @@ int main() {
     report("spmv_exec COO unsupported", spmv_exec<float>(handle, SPMV_FORMAT_COO, &A, dx, dy) ==
                                             SPMV_ERROR_UNSUPPORTED_FORMAT);
 
+    // spmv_exec_transpose (spmv_api.h:70-78): y = A^T x.
+    {
+        std::vector<double> wantT(m, 0.0), scaleT(m, 0.0);
+        for (int r = 0; r < m; ++r)
+            for (int j = A.rowPtr[r]; j < A.rowPtr[r + 1]; ++j) {
+                wantT[A.colIdx[j]] += (double)A.values[j] * x[r];
+                scaleT[A.colIdx[j]] += std::fabs((double)A.values[j] * x[r]);
+            }
+        status = spmv_exec_transpose<float>(handle, SPMV_FORMAT_CSR, &A, dx, dy);
+        cudaStreamSynchronize(st);
+        cudaMemcpy(y.data(), dy, m * sizeof(float), cudaMemcpyDeviceToHost);
+        report("spmv_exec_transpose CSR", status == SPMV_SUCCESS && close(y, wantT, scaleT));
+        report("spmv_exec_transpose CSR5 unsupported",
+               spmv_exec_transpose<float>(handle, SPMV_FORMAT_CSR5, &csr5, dx, dy) == SPMV_ERROR_UNSUPPORTED_FORMAT);
+    }
+
     // column_reorder.cuh: reorderColumns + reorderXVector keep y.
     CSRMatrix<float> B;
     std::vector<int> fmap;
@@ -170,6 +187,23 @@ int main() {
     for (int r = 0; r < m && sorted; ++r)
         for (int j = B.rowPtr[r]; j + 1 < B.rowPtr[r + 1] && sorted; ++j) sorted = B.colIdx[j] <= B.colIdx[j + 1];
     report("sortColumnsWithinRows", sorted);
+
+    // Matrix Market round trip through muxi_spmv::io (src/generators/mtx_io.h).
+    {
+        char path[] = "/tmp/muxi_dropin_XXXXXX";
+        const int fd = mkstemp(path);
+        bool ok = fd >= 0;
+        if (ok) close(fd);
+        ok = ok && io::writeMTXFile<float>(path, B) == SPMV_SUCCESS;
+        io::MTXHeader hdr{};
+        ok = ok && io::readMTXHeader(path, hdr) == SPMV_SUCCESS && hdr.numRows == B.numRows && hdr.nnz == B.nnz;
+        CSRMatrix<float> R;
+        ok = ok && io::readMTXFile<float>(path, R) == SPMV_SUCCESS && R.nnz == B.nnz;
+        for (int r = 0; ok && r <= B.numRows; ++r) ok = R.rowPtr[r] == B.rowPtr[r];
+        for (int j = 0; ok && j < B.nnz; ++j) ok = R.colIdx[j] == B.colIdx[j] && R.values[j] == B.values[j];
+        std::remove(path);
+        report("io::writeMTXFile + io::readMTXFile", ok);
+    }
 
     spmv_destroy_handle(handle);
     cudaStreamDestroy(st);

@@ -1,0 +1,88 @@
+"""Transpose SpMV y = alpha*A^T*x + beta*y (the reference's declared
+spmv_exec_transpose, spmv_api.h:70-78; its transpose kernel scatters with
+float atomics, spmv_csr.cuh:105-107): the device transpose is bit-exact
+against a numpy stable transpose, and y against the FP64 oracle run on
+that transpose, bound 1e-5 (FP32) / 1e-13 (FP64) times sum |a x| per row."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import device_csr, tol_for
+
+pytestmark = pytest.mark.gpu
+
+
+def np_transpose(rp, ci, v, cols):
+    rows = np.repeat(np.arange(len(rp) - 1, dtype=np.int64), np.diff(rp))
+    order = np.argsort(ci, kind="stable")
+    trp = np.zeros(cols + 1, np.int64)
+    np.add.at(trp, ci.astype(np.int64) + 1, 1)
+    return np.cumsum(trp).astype(np.int32), rows[order].astype(np.int32), v[order]
+
+
+def cases(mx):
+    from muxi_spmv_gb300 import workloads as W
+    out = {}
+    s = W.scaled("powerlaw8m", 30000, seed=21)
+    out["powerlaw"] = (*mx.generate(s), s.numCols)
+    s = W.spec("poisson16k")
+    out["poisson"] = (*mx.generate(s), s.numCols)
+    rng = np.random.default_rng(4)
+    lens = np.r_[np.zeros(20), rng.integers(0, 5, 700), np.zeros(9)].astype(np.int32)  # empty rows
+    rp = np.r_[0, np.cumsum(lens)].astype(np.int32)
+    ci = np.concatenate([np.sort(rng.choice(2000, l, replace=False)) for l in lens]).astype(np.int32)
+    out["rect_empty_cols"] = (rp, ci, rng.standard_normal(rp[-1]).astype(np.float32), 2000)
+    out["no_nnz"] = (np.zeros(11, np.int32), np.zeros(0, np.int32), np.zeros(0, np.float32), 6)
+    return out
+
+
+@pytest.fixture(scope="module")
+def mats(mx, cuda):
+    return cases(mx)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_transpose_arrays_bit_exact(mx, cuda, mats, dtype):
+    for name, (rp, ci, v, cols) in mats.items():
+        A = device_csr(mx, rp, ci, v.astype(dtype), cols)
+        B = mx.csr_transpose(A)
+        cuda.cuda.synchronize()
+        trp, tci, tv = np_transpose(rp, ci, v.astype(dtype), cols)
+        assert np.array_equal(B.d_rowPtr.cpu().numpy(), trp), name
+        assert np.array_equal(B.d_colIdx.cpu().numpy()[:len(tci)], tci), name
+        assert np.array_equal(B.d_values.cpu().numpy()[:len(tv)], tv), name
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_transpose_spmv_matches_oracle(mx, cuda, mats, dtype):
+    for name, (rp, ci, v, cols) in mats.items():
+        rows = len(rp) - 1
+        v = v.astype(dtype)
+        A = device_csr(mx, rp, ci, v, cols)
+        xh = mx.gen_vector(rows, 31, dtype=dtype)
+        trp, tci, tv = np_transpose(rp, ci, v, cols)
+        y_ref, absum = oracle.spmv_ref(trp, tci, tv, xh)
+        for alpha, beta in ((1.0, 0.0), (-2.0, 0.5)):
+            y0 = mx.gen_vector(cols, 8, dtype=dtype)
+            y = cuda.from_numpy(y0.copy()).cuda() if cols else cuda.zeros(1, device="cuda")
+            mx.spmv_csr_transpose(A, cuda.from_numpy(xh).cuda() if rows else cuda.zeros(1, device="cuda"), y,
+                                  alpha, beta)
+            cuda.cuda.synchronize()
+            got = y.cpu().numpy()[:cols].astype(np.float64)
+            want = alpha * y_ref + beta * y0.astype(np.float64)
+            bound = tol_for(dtype) * (abs(alpha) * absum + abs(beta * y0.astype(np.float64)))
+            assert (np.abs(got - want) <= bound + (0 if dtype == np.float64 else 1e-30)).all(), (name, alpha)
+
+
+def test_transpose_is_deterministic(mx, cuda, mats):
+    rp, ci, v, cols = mats["powerlaw"]
+    A = device_csr(mx, rp, ci, v, cols)
+    x = cuda.from_numpy(mx.gen_vector(len(rp) - 1, 3)).cuda()
+    ys = []
+    for _ in range(3):
+        y = cuda.empty(cols, device="cuda")
+        mx.spmv_csr_transpose(A, x, y)
+        ys.append(y.cpu().numpy())
+    assert all(np.array_equal(ys[0], b) for b in ys[1:])
