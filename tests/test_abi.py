@@ -84,9 +84,12 @@ def test_argument_errors_without_device(mx):
     assert st == -1
     st = L.spmv_merge_partitions(10, 10, 0, None, None)
     assert st == -2
-    o.operation = 1
+    o.operation = 2  # conjugate: real types only
     st = L.spmv_csr_f32(4, 4, 0, 1, None, None, None, 1, 1.0, 0.0, C.byref(o))
     assert st == -7
+    o.operation = 1  # transpose: argument checks come before any device work
+    st = L.spmv_csr_f32(4, 4, 3, None, None, None, None, None, 1.0, 0.0, C.byref(o))
+    assert st == -2 and "rowPtr" in mx.last_error()
 
 
 def test_reference_partition_count(mx):
