@@ -51,6 +51,119 @@ csr5_tile_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int
 //     tile's carry.
 //   * Any other tile hands each lane its E consecutive products through
 //     shared memory and runs the CSR5 row logic.
+// Row logic of a tile from its row-start mask, for matrices without empty
+// rows.  The mask holds E 32-bit words for the tile's 32E positions: bit k is
+// set when a row starts at position k (k >= 1); bit 0 of word 0 instead says
+// the tile's last row ends exactly at the tile end.  A lane's first row is
+// rFirst plus the set bits up to its first position (a popcount prefix over
+// the words); a set bit inside the lane closes the current row.  Same
+// results as csr5_tile_rows, without reading rowPtr.
+template <typename T, int E>
+__device__ __forceinline__ void csr5_tile_rows_bits(const T (&p)[E], unsigned word, int rFirst, long long t, int lane,
+                                                    int nnz, T* __restrict__ y, T alpha, T beta, bool bz,
+                                                    int* __restrict__ carryRow, T* __restrict__ carryVal) {
+    constexpr int SIGMA = 32 * E;
+    const int tStart = (int)t * SIGMA;
+    const int tEnd = min(tStart + SIGMA, nnz);
+    // lanes l and l+E, l+2E, ... hold word l % E
+    const bool endsAtTileEnd = (__shfl_sync(kFull, word, 0) & 1u) != 0;
+    const unsigned clean = (lane % E == 0) ? (word & ~1u) : word;
+    const int pc = __popc(clean);
+    int incl = pc;
+#pragma unroll
+    for (int off = 1; off < E; off <<= 1) {
+        const int v = __shfl_up_sync(kFull, incl, off, E);
+        if (lane % E >= off) incl += v;
+    }
+    const int w = (E * lane) >> 5, o = (E * lane) & 31;
+    const unsigned wordW = __shfl_sync(kFull, clean, w);
+    const int exclW = __shfl_sync(kFull, incl - pc, w);
+    const unsigned upTo = (o + 1 >= 32) ? 0xffffffffu : ((1u << (o + 1)) - 1u);
+    const int startRow = rFirst + exclW + __popc(wordW & upTo);
+    const unsigned myBits = (wordW >> o) & (E >= 32 ? 0xffffffffu : ((1u << E) - 1u));
+    const unsigned nextFirst = __shfl_down_sync(kFull, myBits & 1u, 1);
+
+    const int j0 = tStart + lane * E;
+    const int laneEnd = min(j0 + E, tEnd);
+    const bool has = j0 < tEnd;
+    int key = has ? startRow : 0x7fffffff;  // lanes without elements sort last in the scan
+    int headRow = -1;
+    T run = T(0), headVal = T(0);
+    if (has) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            if (j0 + e < laneEnd) {
+                if (e > 0 && ((myBits >> e) & 1u)) {  // a row starts here: the current one is complete
+                    if (headRow < 0) {
+                        headRow = key;
+                        headVal = run;
+                    } else {
+                        y[key] = axpby(alpha, run, beta, bz, y + key);
+                    }
+                    ++key;
+                    run = T(0);
+                }
+                run += p[e];
+            }
+        }
+    }
+    // does the lane's last row end at its last element?
+    const bool endsHere = laneEnd == tEnd ? endsAtTileEnd : (lane < 31 && nextFirst != 0u);
+
+    T incl2 = run;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int k2 = __shfl_up_sync(kFull, key, off);
+        const T v2 = __shfl_up_sync(kFull, incl2, off);
+        if (lane >= off && k2 == key) incl2 += v2;
+    }
+    const int prevKey = __shfl_up_sync(kFull, key, 1);
+    const T prevIncl = __shfl_up_sync(kFull, incl2, 1);
+    if (!has) return;
+    const T cin = (lane > 0 && prevKey == startRow) ? prevIncl : T(0);
+    if (headRow >= 0) y[headRow] = axpby(alpha, headVal + cin, beta, bz, y + headRow);
+    if (endsHere) y[key] = axpby(alpha, incl2, beta, bz, y + key);
+    if (laneEnd == tEnd) {  // the lane holding the tile's last nonzero
+        carryRow[t] = endsHere ? -1 : key;
+        carryVal[t] = incl2;
+    }
+}
+
+// Row-start masks of a CSR5 tiling (see csr5_tile_rows_bits); matrices
+// without empty rows only.  bits: tiles * E words, zeroed before.
+__global__ void tile_bits_kernel(const int* __restrict__ rowPtr, int numRows, int sigma, int words, long long tiles,
+                                 unsigned* __restrict__ bits) {
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0) atomicOr(bits + (tiles - 1) * words, 1u);  // the last tile's last row ends at its end
+    if (r < 1 || r >= numRows) return;
+    const int pos = rowPtr[r];
+    const long long t = pos / sigma;
+    const int k = pos - (int)(t * sigma);
+    if (k) atomicOr(bits + t * words + (k >> 5), 1u << (k & 31));
+    else atomicOr(bits + (t - 1) * words, 1u);  // row r starts tile t: tile t-1's last row ends at its end
+}
+
+spmv_status_t csr5_tile_bits(const int* rowPtr, int numRows, int sigma, long long tiles, void** buf, cudaStream_t s) {
+    *buf = nullptr;
+    if (tiles <= 0) return SPMV_SUCCESS;
+    const int words = sigma / 32;
+    const size_t bytes = sizeof(unsigned) * (size_t)tiles * words;
+    MXS_CUDA(cudaMalloc(buf, bytes));
+    cudaError_t e = cudaMemsetAsync(*buf, 0, bytes, s);
+    if (e == cudaSuccess) {
+        tile_bits_kernel<<<grid_for(numRows > 0 ? numRows : 1, 256), 256, 0, s>>>(rowPtr, numRows, sigma, words,
+                                                                                 tiles, static_cast<unsigned*>(*buf));
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaFree(*buf);
+        *buf = nullptr;
+        return cuda_fail(e, "tile row masks", __FILE__, __LINE__);
+    }
+    return SPMV_SUCCESS;
+}
+
 // sRp / sP: this warp's shared regions (kOrderedRpCap ints, 32E values).
 // The rowPtr slice holds up to kOrderedRpCap entries (tiles spanning up to
 // 62 rows, nine in ten of the general tiles of a power-law matrix); a tile
@@ -60,6 +173,7 @@ constexpr int kOrderedRpCap = 64;
 template <typename T, int E>
 struct OrderedLoad {
     int rFirst, rLast;
+    unsigned bits;  // word (lane % E) of the tile's row-start mask (when the plan has masks)
     int c[E];
     T v[E];
 };
@@ -67,9 +181,11 @@ struct OrderedLoad {
 template <typename T, int E>
 __device__ __forceinline__ void csr5_ordered_load(OrderedLoad<T, E>& L, long long t, int lane, int numRows, int nnz,
                                                   const int* __restrict__ colIdx, const T* __restrict__ values,
-                                                  const int* __restrict__ tileRow, long long tiles) {
+                                                  const int* __restrict__ tileRow, long long tiles,
+                                                  const unsigned* __restrict__ tileBits) {
     constexpr int SIGMA = 32 * E;
     const int tStart = (int)t * SIGMA;
+    L.bits = tileBits ? __ldg(tileBits + t * E + (lane % E)) : 0u;
     if (tStart + SIGMA <= nnz) {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
@@ -94,7 +210,7 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
                                                      const int* __restrict__ rowPtr, const T* __restrict__ x,
                                                      T* __restrict__ y, T alpha, T beta, bool bz, long long tiles,
                                                      int* __restrict__ carryRow, T* __restrict__ carryVal,
-                                                     bool noEmpty, int* sRp, T* sP) {
+                                                     bool noEmpty, int* sRp, T* sP, bool useBits) {
     const int rFirst = L.rFirst, rLast = L.rLast;
     T g[E];
 #pragma unroll
@@ -112,6 +228,17 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
         return;
     }
 
+    if (useBits) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) sP[lane + 32 * e] = L.v[e] * g[e];
+        __syncwarp();
+        T p[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) p[e] = sP[lane * E + e];
+        csr5_tile_rows_bits<T, E>(p, L.bits, rFirst, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal);
+        if (REUSE) __syncwarp();
+        return;
+    }
     const int nRp = rLast - rFirst + 2;
     const bool staged = nRp <= kOrderedRpCap;
     if (staged) {
@@ -140,11 +267,11 @@ __device__ __forceinline__ void csr5_ordered_tile(long long t, int lane, int num
                                                   T* __restrict__ y, T alpha, T beta, bool bz,
                                                   const int* __restrict__ tileRow, long long tiles,
                                                   int* __restrict__ carryRow, T* __restrict__ carryVal, bool noEmpty,
-                                                  int* sRp, T* sP) {
+                                                  const unsigned* __restrict__ tileBits, int* sRp, T* sP) {
     OrderedLoad<T, E> L;
-    csr5_ordered_load<T, E>(L, t, lane, numRows, nnz, colIdx, values, tileRow, tiles);
+    csr5_ordered_load<T, E>(L, t, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
     csr5_ordered_compute<T, E, false>(L, t, lane, nnz, rowPtr, x, y, alpha, beta, bz, tiles, carryRow, carryVal,
-                                      noEmpty, sRp, sP);
+                                      noEmpty, sRp, sP, tileBits != nullptr);
 }
 
 // One tile per warp, BLOCK threads per block, MINB resident blocks per SM
@@ -156,7 +283,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
 csr5_ordered_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int* __restrict__ colIdx,
                     const T* __restrict__ values, const T* __restrict__ x, T* __restrict__ y, T alpha, T beta,
                     int betaZero, const int* __restrict__ tileRow, long long tiles, int* __restrict__ carryRow,
-                    T* __restrict__ carryVal, int noEmptyRows) {
+                    T* __restrict__ carryVal, int noEmptyRows, const unsigned* __restrict__ tileBits) {
     constexpr int WARPS = BLOCK / 32;
     __shared__ int sRpAll[WARPS][kOrderedRpCap];
     __shared__ __align__(16) T sPAll[WARPS][32 * E];
@@ -164,7 +291,8 @@ csr5_ordered_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const 
     if (t >= tiles) return;  // uniform per warp
     const int w = threadIdx.x >> 5;
     csr5_ordered_tile<T, E>(t, threadIdx.x & 31, numRows, nnz, rowPtr, colIdx, values, x, y, alpha, beta,
-                            betaZero != 0, tileRow, tiles, carryRow, carryVal, noEmptyRows != 0, sRpAll[w], sPAll[w]);
+                            betaZero != 0, tileRow, tiles, carryRow, carryVal, noEmptyRows != 0, tileBits, sRpAll[w],
+                            sPAll[w]);
 }
 
 // Persistent: block b takes chunks b, b + gridDim.x, ... of `chunk`
@@ -177,7 +305,8 @@ __global__ void __launch_bounds__(WARPS * 32)
 csr5_ordered_persistent_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int* __restrict__ colIdx,
                                const T* __restrict__ values, const T* __restrict__ x, T* __restrict__ y, T alpha,
                                T beta, int betaZero, const int* __restrict__ tileRow, long long tiles,
-                               int* __restrict__ carryRow, T* __restrict__ carryVal, int noEmptyRows, int chunk) {
+                               int* __restrict__ carryRow, T* __restrict__ carryVal, int noEmptyRows, int chunk,
+                               const unsigned* __restrict__ tileBits) {
     __shared__ int sRpAll[WARPS][kOrderedRpCap];
     __shared__ __align__(16) T sPAll[WARPS][32 * E];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -194,7 +323,7 @@ csr5_ordered_persistent_kernel(int numRows, int nnz, const int* __restrict__ row
     }
     if (t < 0) return;
     OrderedLoad<T, E> cur, nxt;
-    csr5_ordered_load<T, E>(cur, t, lane, numRows, nnz, colIdx, values, tileRow, tiles);
+    csr5_ordered_load<T, E>(cur, t, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
     while (t >= 0) {
         int tn = t + WARPS, chn = ch;
         if (tn >= ntiles || tn >= ch * chunk + chunk) {
@@ -205,9 +334,9 @@ csr5_ordered_persistent_kernel(int numRows, int nnz, const int* __restrict__ row
                 tn = -1;
             }
         }
-        if (tn >= 0) csr5_ordered_load<T, E>(nxt, tn, lane, numRows, nnz, colIdx, values, tileRow, tiles);
+        if (tn >= 0) csr5_ordered_load<T, E>(nxt, tn, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
         csr5_ordered_compute<T, E, true>(cur, t, lane, nnz, rowPtr, x, y, alpha, beta, betaZero != 0, tiles,
-                                         carryRow, carryVal, noEmptyRows != 0, sRpAll[w], sPAll[w]);
+                                         carryRow, carryVal, noEmptyRows != 0, sRpAll[w], sPAll[w], tileBits != nullptr);
         cur = nxt;
         t = tn;
         ch = chn;
@@ -335,7 +464,7 @@ __global__ void csr5_fixup_kernel(long long tiles, const int* __restrict__ carry
 
 template <typename T, int E, int WARPS>
 static spmv_status_t launch_ordered_persistent(const int* tileRow, long long tiles, int* carryRow, T* carryVal,
-                                               const RowsArgs<T>& a, int chunk, cudaStream_t s) {
+                                               const RowsArgs<T>& a, int chunk, const unsigned* bits, cudaStream_t s) {
     static int perSM = -1;  // resident blocks per SM of this instantiation
     if (perSM < 0) {
         int n = 0;
@@ -347,19 +476,19 @@ static spmv_status_t launch_ordered_persistent(const int* tileRow, long long til
     if (g > chunks) g = chunks;
     csr5_ordered_persistent_kernel<T, E, WARPS><<<(unsigned)g, WARPS * 32, 0, s>>>(
         a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha, a.beta, a.betaZero, tileRow, tiles,
-        carryRow, carryVal, a.noEmptyRows, chunk);
+        carryRow, carryVal, a.noEmptyRows, chunk, bits);
     return SPMV_SUCCESS;
 }
 
 template <typename T, int E>
 static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* carryRow, T* carryVal,
-                                    const RowsArgs<T>& a, int block, int chunk, cudaStream_t s) {
+                                    const RowsArgs<T>& a, int block, int chunk, const unsigned* bits, cudaStream_t s) {
     if (chunk <= 0) {
         constexpr bool wide = E * sizeof(T) >= 64;  // 16 doubles or floats per lane: fewer, larger blocks
 #define MXS_ORDERED(B, M)                                                                                        \
     csr5_ordered_kernel<T, E, B, M><<<grid_for(tiles * 32, B), B, 0, s>>>(                                        \
         a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha, a.beta, a.betaZero, tileRow, tiles,   \
-        carryRow, carryVal, a.noEmptyRows)
+        carryRow, carryVal, a.noEmptyRows, bits)
         switch (block) {
             case 128: MXS_ORDERED(128, wide ? 6 : 16); break;
             case 256: MXS_ORDERED(256, wide ? 3 : 6); break;
@@ -371,9 +500,9 @@ static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* ca
         return SPMV_SUCCESS;
     }
     switch (block) {
-        case 256: return launch_ordered_persistent<T, E, 8>(tileRow, tiles, carryRow, carryVal, a, chunk, s);
-        case 512: return launch_ordered_persistent<T, E, 16>(tileRow, tiles, carryRow, carryVal, a, chunk, s);
-        case 1024: return launch_ordered_persistent<T, E, 32>(tileRow, tiles, carryRow, carryVal, a, chunk, s);
+        case 256: return launch_ordered_persistent<T, E, 8>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, s);
+        case 512: return launch_ordered_persistent<T, E, 16>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, s);
+        case 1024: return launch_ordered_persistent<T, E, 32>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, s);
         default: MXS_FAIL(SPMV_ERROR_INTERNAL, "persistent CSR5 block must be 256, 512 or 1024 (got %d)", block);
     }
 }
@@ -381,11 +510,11 @@ static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* ca
 template <typename T>
 spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
                        const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain, bool ordered, int block,
-                       int chunk, const Csr5Chains* chains) {
+                       int chunk, const Csr5Chains* chains, const unsigned* tileBits) {
     if (ordered) {
-        if (sigma == 128) MXS_TRY((launch_ordered<T, 4>(tileRow, tiles, carryRow, carryVal, a, block, chunk, s)));
-        else if (sigma == 256) MXS_TRY((launch_ordered<T, 8>(tileRow, tiles, carryRow, carryVal, a, block, chunk, s)));
-        else if (sigma == 512) MXS_TRY((launch_ordered<T, 16>(tileRow, tiles, carryRow, carryVal, a, block, chunk, s)));
+        if (sigma == 128) MXS_TRY((launch_ordered<T, 4>(tileRow, tiles, carryRow, carryVal, a, block, chunk, tileBits, s)));
+        else if (sigma == 256) MXS_TRY((launch_ordered<T, 8>(tileRow, tiles, carryRow, carryVal, a, block, chunk, tileBits, s)));
+        else if (sigma == 512) MXS_TRY((launch_ordered<T, 16>(tileRow, tiles, carryRow, carryVal, a, block, chunk, tileBits, s)));
         else MXS_FAIL(SPMV_ERROR_INTERNAL, "CSR5 sigma must be 128, 256 or 512 (got %d)", sigma);
     } else {
         const unsigned g = grid_for(tiles * 32, 256);
@@ -428,9 +557,11 @@ template spmv_status_t run_csr5_fixup<float>(long long, const int*, const float*
 template spmv_status_t run_csr5_fixup<double>(long long, const int*, const double*, const RowsArgs<double>&,
                                               cudaStream_t);
 template spmv_status_t run_csr5<float>(int, const int*, long long, int*, float*, const RowsArgs<float>&,
-                                       cudaStream_t, cudaEvent_t, bool, int, int, const Csr5Chains*);
+                                       cudaStream_t, cudaEvent_t, bool, int, int, const Csr5Chains*,
+                                       const unsigned*);
 template spmv_status_t run_csr5<double>(int, const int*, long long, int*, double*, const RowsArgs<double>&,
-                                        cudaStream_t, cudaEvent_t, bool, int, int, const Csr5Chains*);
+                                        cudaStream_t, cudaEvent_t, bool, int, int, const Csr5Chains*,
+                                        const unsigned*);
 
 // ---------------------------------------------------------------------------
 // ELL

@@ -29,7 +29,12 @@ spmv_status_t csr5_chains(const int* rowPtr, int numRows, int nnz, int sigma, co
 template <typename T>
 spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
                        const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain = nullptr, bool ordered = false,
-                       int block = 256, int chunk = 0, const Csr5Chains* chains = nullptr);
+                       int block = 256, int chunk = 0, const Csr5Chains* chains = nullptr,
+                       const unsigned* tileBits = nullptr);
+
+// Row-start masks of a CSR5 tiling for an ordered plan (matrices without
+// empty rows): sigma/32 words per tile, one cudaMalloc'd buffer in *buf.
+spmv_status_t csr5_tile_bits(const int* rowPtr, int numRows, int sigma, long long tiles, void** buf, cudaStream_t s);
 
 // Adds the carries of rows split between CSR5 tiles, in tile order.
 template <typename T>

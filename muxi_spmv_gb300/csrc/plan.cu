@@ -92,7 +92,8 @@ static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T
         case SPMV_KERNEL_CSR5:
             MXS_TRY(run_csr5<T>(32 * v.itemsPerThread, p->csr5TileRow, p->csr5Tiles, p->csr5CarryRow,
                                 static_cast<T*>(p->csr5CarryVal), a, s, evEnd, v.vectorWidth == 32, v.blockSize,
-                                v.vectorWidth == 32 ? v.threadsPerRow : 0, &p->chains));
+                                v.vectorWidth == 32 ? v.threadsPerRow : 0, &p->chains,
+                                static_cast<const unsigned*>(p->tileBits)));
             break;
         case SPMV_KERNEL_ELL:
             MXS_TRY(run_ell<T>(p->numRows, p->ellWidth, p->ellCol, static_cast<const T*>(p->ellVal), x, y, alpha, beta,
@@ -219,6 +220,8 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
                 p->noEmptyRows = st == SPMV_SUCCESS && empties == 0;
                 if (st == SPMV_SUCCESS && v.kernel == SPMV_KERNEL_CSR5)
                     st = csr5_chains(rowPtr, R, N, sigma, p->csr5TileRow, T, &p->chainBuf, &p->chains, h->stream);
+                if (st == SPMV_SUCCESS && v.kernel == SPMV_KERNEL_CSR5 && v.vectorWidth == 32 && p->noEmptyRows)
+                    st = csr5_tile_bits(rowPtr, R, sigma, T, &p->tileBits, h->stream);
                 if (st == SPMV_SUCCESS) {
                     e = cudaStreamSynchronize(h->stream);
                     if (e != cudaSuccess) st = cuda_fail(e, "plan build", __FILE__, __LINE__);
@@ -268,6 +271,7 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
         if (p->mergeBuf) cudaFree(p->mergeBuf);
         if (p->csr5Buf) cudaFree(p->csr5Buf);
         if (p->chainBuf) cudaFree(p->chainBuf);
+        if (p->tileBits) cudaFree(p->tileBits);
         if (p->ellBuf) cudaFree(p->ellBuf);
         delete p;
         return st;
@@ -325,6 +329,7 @@ spmv_status_t spmv_plan_destroy(spmv_plan_t p) {
     if (p->mergeBuf) cudaFree(p->mergeBuf);
     if (p->csr5Buf) cudaFree(p->csr5Buf);
     if (p->chainBuf) cudaFree(p->chainBuf);
+    if (p->tileBits) cudaFree(p->tileBits);
     if (p->ellBuf) cudaFree(p->ellBuf);
     delete p;
     return SPMV_SUCCESS;

@@ -30,6 +30,7 @@ struct spmv_plan_s {
     int* errFlag = nullptr;  // device word raised by a pipelined kernel whose wait gave up
     bool noEmptyRows = false;  // checked at plan creation (CSR5 kernels skip the empty-row pass)
     void* chainBuf = nullptr;  // CSR5 carry chains (start / end / row), see Csr5Chains
+    void* tileBits = nullptr;  // ordered CSR5 on a matrix without empty rows: row-start masks
     mxs::Csr5Chains chains{};
     // ELL: column-major copy of the matrix
     int ellWidth = 0;
