@@ -272,14 +272,46 @@ def gpu_arm(args):
             e2e_step()
         f1.record(stream)
     torch.cuda.synchronize(dev)
-    e2e_ms = f0.elapsed_time(f1) / args.steps
+    serial_ms = f0.elapsed_time(f1) / args.steps
     plan.device_error()
+
+    # ---- end to end through the host pipeline (spmv_pipeline_*): each
+    # request copies its own x in and its y out; copies overlap the SpMV of
+    # the same request (row slices) and of the neighbouring requests.
+    pipe_info, pipe_parity = None, None
+    e2e_ms = serial_ms
+    if perm is None and not args.no_pipeline:
+        pipe = mx.Pipeline(h, A, plan.variant, slices=args.slices, depth=args.depth)
+        pipe_info = pipe.info()
+        xs = [x_pin, torch.from_numpy(mx.gen_vector(A.numCols, 77, dtype=dtype)).pin_memory()]
+        ys = [torch.empty(A.numRows, dtype=tdt).pin_memory() for _ in range(2)]
+        for i in range(max(1, args.warmup)):
+            pipe.submit(xs[i % 2], ys[i % 2])
+        pipe.wait()
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        pipe.order_after(stream)
+        for i in range(args.steps):  # the last request takes xs[0], the x of the parity check
+            j = (args.steps - 1 - i) % 2
+            pipe.submit(xs[j], ys[j])
+        pipe.join(stream)
+        g1.record(stream)
+        torch.cuda.synchronize(dev)
+        pipe.wait()
+        e2e_ms = g0.elapsed_time(g1) / args.steps
+        r = oracle.row_errors(ys[0].numpy(), y_ref, absum, 1e-5 if dtype == np.float32 else 1e-13)
+        pipe_parity = {"rows_checked": int(A.numRows), "max_err_over_bound": float(r.max()),
+                       "rows_out_of_bound": int((r > 1).sum())}
+        if pipe_parity["rows_out_of_bound"]:
+            print(f"PIPELINE PARITY FAILURE: {pipe_parity}", file=sys.stderr)
+        pipe.destroy()
     clocks.stop()
 
     if ws > 1:
-        t = torch.tensor([step_ms, e2e_ms], device=dev)
+        t = torch.tensor([step_ms, e2e_ms, serial_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms, e2e_ms = t.tolist()
+        step_ms, e2e_ms, serial_ms = t.tolist()
         dist.barrier()
 
     peak, peak_kind = peaks()
@@ -287,6 +319,7 @@ def gpu_arm(args):
     achieved = nbytes / (kern_ms * 1e-3) / 1e9
     value = ws * nbytes / (step_ms * 1e-3) / 1e9
     e2e_val = ws * nbytes / (e2e_ms * 1e-3) / 1e9
+    serial_val = ws * nbytes / (serial_ms * 1e-3) / 1e9
     pv = plan.variant.as_dict()
     kern_names = {mx.KERNEL_MERGE: "merge_vec_kernel",
                   mx.KERNEL_CSR5: "csr5_ordered_kernel" if pv["vectorWidth"] == 32 else "csr5_tile_kernel",
@@ -317,8 +350,14 @@ def gpu_arm(args):
                          "kernel_ms": round(kern_ms, 5), "traffic": traffic},
             "e2e": {"value": round(e2e_val, 3), "unit": UNIT, "h2d_bytes_per_step": int(A.numCols * vs),
                     "d2h_bytes_per_step": int(A.numRows * vs), "ms_per_step": round(e2e_ms, 5),
-                    "call": "spmv_plan_exec_f32 with host x/y copied in the timed region"},
-            "gpu_launches": args.steps * launches_per_step * 2,
+                    "call": ("spmv_pipeline_submit: pinned host x in, pinned host y out, copies overlapped "
+                             f"({pipe_info['slices']} row slices, {pipe_info['depth']} requests in flight)"
+                             if pipe_info else "spmv_plan_exec with host x/y copied in the timed region"),
+                    "serial": {"value": round(serial_val, 3), "ms_per_step": round(serial_ms, 5),
+                               "call": "H2D(x), spmv_plan_exec, D2H(y) in order on one stream"},
+                    "pipeline_parity": pipe_parity},
+            "gpu_launches": args.steps * launches_per_step * 2 +
+                            (args.steps * pipe_info["launches_per_request"] if pipe_info else 0),
             "clocks": clocks.summary(), "parity": parity}
 
     if rank == 0 and not args.no_cpu_baseline:
@@ -565,6 +604,9 @@ def main():
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
     ap.add_argument("--variant", default="", help="kernel,block,tpr,ipt,vec (spmv_variant_t)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-pipeline", action="store_true", help="e2e through one stream, copies not overlapped")
+    ap.add_argument("--slices", type=int, default=1, help="host pipeline row slices")
+    ap.add_argument("--depth", type=int, default=2, help="host pipeline requests in flight")
     ap.add_argument("--scale-rows", type=int, default=0, help="same law on this many rows (profiling cases)")
     ap.add_argument("--colperm", default="none", choices=["none", "com", "minrow", "freq"],
                     help="reorder columns first (centre of mass, the reference's min-row 'RCM', frequency)")

@@ -657,6 +657,50 @@ SPMV_API spmv_status_t spmv_batch_exec_f32(spmv_handle_t* handle, spmv_batch_t b
                                            spmv_batch_mode_t mode);
 SPMV_API spmv_status_t spmv_batch_info(spmv_batch_t batch, long long* tiles, int* warps, long long* nnzTotal);
 
+/* ------------------------------------------------------------------ */
+/* Host-to-host pipeline: x in pinned host memory -> y in pinned host   */
+/* memory, with the copies overlapping the SpMV.  Replaces the pinned-  */
+/* memory / multi-stream path of tests/test_pinned_memory.cu:245-380    */
+/* (testPinnedAsync, testPinnedMultiStream: one stream per row range,   */
+/* whole-vector copies before and after the kernels).                   */
+/*                                                                      */
+/* The matrix (device CSR, borrowed) is cut into `slices` row slices of  */
+/* equal rows + nonzeros; slice s of y is copied out as soon as slice s  */
+/* is computed, while later slices run.  Up to `depth` requests are in  */
+/* flight, each with its own device x and y, so the next request's x    */
+/* copy runs under the current SpMV.  Every slice runs the variant       */
+/* chosen for the whole matrix (NULL or AUTO: as spmv_plan_create).     */
+/* slices <= 0: 1; depth <= 0: 2 (limits 256 and 8).  Throughput comes  */
+/* from depth >= 2 (copies hidden under the neighbouring requests);     */
+/* slices > 1 shorten one request's latency at about 5 us per slice.    */
+/*                                                                      */
+/* submit only enqueues work (on the pipeline's own streams): hx must    */
+/* stay unchanged and hy unread until spmv_pipeline_wait returns.  With  */
+/* pageable host memory the copies are correct but do not overlap.  With */
+/* beta != 0 hy is read (copied in) before the request's SpMV.           */
+/* ------------------------------------------------------------------ */
+typedef struct spmv_pipeline_s* spmv_pipeline_t;
+
+SPMV_API spmv_status_t spmv_pipeline_create(spmv_handle_t* handle, spmv_type_t type, int numRows, int numCols,
+                                            int nnz, const int* rowPtr, const int* colIdx, const void* values,
+                                            const spmv_variant_t* variant, int slices, int depth,
+                                            spmv_pipeline_t* pipeline);
+SPMV_API spmv_status_t spmv_pipeline_destroy(spmv_pipeline_t pipeline);
+SPMV_API spmv_status_t spmv_pipeline_submit_f32(spmv_pipeline_t pipeline, float alpha, const float* hx, float beta,
+                                                float* hy);
+SPMV_API spmv_status_t spmv_pipeline_submit_f64(spmv_pipeline_t pipeline, double alpha, const double* hx,
+                                                double beta, double* hy);
+/* Waits for every submitted request (their hy are then complete). */
+SPMV_API spmv_status_t spmv_pipeline_wait(spmv_pipeline_t pipeline);
+/* Later submissions start after the work queued on `stream` so far. */
+SPMV_API spmv_status_t spmv_pipeline_order_after(spmv_pipeline_t pipeline, cudaStream_t stream);
+/* Work queued on `stream` from now on waits for every submitted request. */
+SPMV_API spmv_status_t spmv_pipeline_join(spmv_pipeline_t pipeline, cudaStream_t stream);
+/* Slices kept (boundaries inside one row are dropped), depth, the slices'
+ * variant, device bytes held, kernel launches per request. */
+SPMV_API spmv_status_t spmv_pipeline_info(spmv_pipeline_t pipeline, int* slices, int* depth,
+                                          spmv_variant_t* variant, size_t* deviceBytes, int* launchesPerRequest);
+
 #ifdef __cplusplus
 }
 #endif

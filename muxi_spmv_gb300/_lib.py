@@ -186,6 +186,15 @@ SIGNATURES = {
     "spmv_batch_set_vectors_f32": (S, [P, C.POINTER(P), C.POINTER(P)]),
     "spmv_batch_exec_f32": (S, [C.POINTER(Handle), P, F, F, I]),
     "spmv_batch_info": (S, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
+    "spmv_pipeline_create": (S, [C.POINTER(Handle), I, I, I, I, P, P, P, C.POINTER(Variant), I, I, C.POINTER(P)]),
+    "spmv_pipeline_destroy": (S, [P]),
+    "spmv_pipeline_submit_f32": (S, [P, F, P, F, P]),
+    "spmv_pipeline_submit_f64": (S, [P, D, P, D, P]),
+    "spmv_pipeline_wait": (S, [P]),
+    "spmv_pipeline_order_after": (S, [P, P]),
+    "spmv_pipeline_join": (S, [P, P]),
+    "spmv_pipeline_info": (S, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(Variant),
+                               C.POINTER(C.c_size_t), C.POINTER(C.c_int)]),
 }
 
 BATCH_PERSISTENT, BATCH_PERSISTENT_GRAPH, BATCH_LOOP, BATCH_LOOP_GRAPH = range(4)

@@ -280,6 +280,62 @@ class Plan:
             pass
 
 
+class Pipeline:
+    """Host-to-host SpMV: x from pinned host memory, y to pinned host memory,
+    copies overlapped with the SpMV (row slices copied out as they finish,
+    `depth` requests in flight).  The pinned-memory / multi-stream path of the
+    reference's tests/test_pinned_memory.cu:245-380."""
+
+    def __init__(self, handle: SpmvHandle, A: CSRMatrix, variant: Variant | None = None, slices: int = 0,
+                 depth: int = 0):
+        self.handle = handle
+        self.A = A
+        p = C.c_void_p()
+        check(lib().spmv_pipeline_create(handle.raw, SPMV_TYPE_FLOAT if _is_f32(A) else SPMV_TYPE_DOUBLE,
+                                         *A.device_args(), C.byref(variant) if variant is not None else None,
+                                         slices, depth, C.byref(p)), "spmv_pipeline_create")
+        self._p = p
+        self._held = []  # host tensors of requests in flight
+
+    def info(self) -> dict:
+        sl, dp, lp = C.c_int(), C.c_int(), C.c_int()
+        v, b = Variant(), C.c_size_t()
+        check(lib().spmv_pipeline_info(self._p, C.byref(sl), C.byref(dp), C.byref(v), C.byref(b), C.byref(lp)),
+              "spmv_pipeline_info")
+        return {"slices": sl.value, "depth": dp.value, "variant": v.as_dict(), "device_bytes": b.value,
+                "launches_per_request": lp.value}
+
+    def submit(self, hx, hy, alpha=1.0, beta=0.0):
+        """Enqueues y = alpha*A*x + beta*y for host tensors hx, hy (pinned for
+        overlap); hy is complete after wait()."""
+        f = lib().spmv_pipeline_submit_f32 if _is_f32(self.A) else lib().spmv_pipeline_submit_f64
+        check(f(self._p, alpha, _ptr(hx), beta, _ptr(hy)), "spmv_pipeline_submit")
+        self._held.append((hx, hy))
+        return hy
+
+    def wait(self):
+        check(lib().spmv_pipeline_wait(self._p), "spmv_pipeline_wait")
+        self._held.clear()
+
+    def order_after(self, stream):
+        check(lib().spmv_pipeline_order_after(self._p, _stream_ptr(stream)), "spmv_pipeline_order_after")
+
+    def join(self, stream):
+        check(lib().spmv_pipeline_join(self._p, _stream_ptr(stream)), "spmv_pipeline_join")
+
+    def destroy(self):
+        if self._p:
+            check(lib().spmv_pipeline_destroy(self._p), "spmv_pipeline_destroy")
+            self._p = None
+            self._held.clear()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
 # ---------------------------------------------------------------------------
 # CSR5 (src/spmv/csr5/spmv_csr5.cuh, src/formats/sparse_formats.h:284-386)
 # ---------------------------------------------------------------------------

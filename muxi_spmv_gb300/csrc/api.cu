@@ -215,6 +215,7 @@ static spmv_status_t csr_exec(const spmv_variant_t* v, int R, int C, int N, cons
         case SPMV_KERNEL_MERGE:
         case SPMV_KERNEL_AUTO: {
             MergeGeom g = v->kernel == SPMV_KERNEL_AUTO ? kDefaultMerge : merge_geom_of(*v);
+            if (g.vec && !(aligned16(colIdx) && aligned16(values))) g = merge_unaligned_geom(g);
             if (!merge_geom_supported(g))
                 MXS_FAIL(SPMV_ERROR_INTERNAL, "unsupported merge shape block=%d ipt=%d", g.block, g.ipt);
             MXS_TRY(merge_stateless<T>(g, a, s));

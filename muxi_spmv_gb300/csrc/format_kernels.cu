@@ -511,6 +511,14 @@ template <typename T>
 spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
                        const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain, bool ordered, int block,
                        int chunk, const Csr5Chains* chains, const unsigned* tileBits) {
+    // The lane-contiguous kernel reads 16-byte quads; on arrays that are not
+    // 16-byte aligned the ordered kernel (4-byte loads) runs the same tiles.
+    if (!ordered && !(aligned16(a.colIdx) && aligned16(a.values))) {
+        ordered = true;
+        block = 128;
+        chunk = 0;
+        tileBits = nullptr;
+    }
     if (ordered) {
         if (sigma == 128) MXS_TRY((launch_ordered<T, 4>(tileRow, tiles, carryRow, carryVal, a, block, chunk, tileBits, s)));
         else if (sigma == 256) MXS_TRY((launch_ordered<T, 8>(tileRow, tiles, carryRow, carryVal, a, block, chunk, tileBits, s)));

@@ -21,6 +21,9 @@ inline cudaStream_t opts_stream(const spmv_opts_t* o) {
     return (o && o->stream) ? reinterpret_cast<cudaStream_t>(o->stream) : (cudaStream_t)0;
 }
 
+// 16-byte loads of colIdx / values need both arrays 16-byte aligned.
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
 // Launch shape helpers.
 inline unsigned grid_for(long long work, int per_block) {
     long long g = (work + per_block - 1) / per_block;

@@ -43,6 +43,9 @@ struct MergeGeom {
 // Builds the geometry of a MERGE variant (defaults filled in).
 MergeGeom merge_geom_of(const spmv_variant_t& v);
 bool merge_geom_supported(const MergeGeom& g);
+// The per-item consumer with the same block size: what runs when a 16-byte
+// vectorised geometry meets colIdx / values that are not 16-byte aligned.
+inline MergeGeom merge_unaligned_geom(const MergeGeom& g) { return MergeGeom{g.block, 7, 0}; }
 // Number of tiles for a matrix: ceil((R+N)/tile), at least 1.
 long long merge_tile_count(int numRows, int nnz, const MergeGeom& g);
 // Bytes of scratch the merge path needs for P tiles and value size vsize:

@@ -53,7 +53,8 @@ extern "C" spmv_status_t spmv_csr_noalloc_f32(int numRows, int numCols, int nnz,
     clear_error();
     if (numRows < 0 || numCols < 0 || nnz < 0)
         MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "negative dimension (R=%d C=%d nnz=%d)", numRows, numCols, nnz);
-    const MergeGeom g{256, 8, 4};
+    MergeGeom g{256, 8, 4};
+    if (nnz > 0 && !(aligned16(colIdx) && aligned16(values))) g = merge_unaligned_geom(g);
     const long long tiles = merge_tile_count(numRows, nnz, g);
     const size_t need = merge_scratch_bytes(tiles, sizeof(float));
     if (need > kNoAllocScratchBytes)

@@ -48,15 +48,12 @@ static spmv_variant_t resolve(const spmv_variant_t* req, int R, int N) {
 }
 
 template <typename T>
-static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T* x, T beta, T* y) {
-    clear_error();
-    if (!h) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "handle is NULL");
+spmv_status_t plan_exec_stream(spmv_plan_t p, T alpha, const T* x, T beta, T* y, cudaStream_t s) {
     if (!p) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "plan is NULL");
     const spmv_type_t want = sizeof(T) == 4 ? SPMV_TYPE_FLOAT : SPMV_TYPE_DOUBLE;
     if (p->type != want) MXS_FAIL(SPMV_ERROR_UNSUPPORTED_TYPE, "plan value type does not match the call");
     if (p->numRows > 0 && !y) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "y is NULL");
     if (p->nnz > 0 && !x) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "x is NULL");
-    const cudaStream_t s = h->stream;
     if (p->numRows == 0) return SPMV_SUCCESS;
     if (p->nnz == 0) return run_scale<T>(p->numRows, y, beta, s);
     RowsArgs<T> a{p->numRows, p->nnz, p->rowPtr, p->colIdx, static_cast<const T*>(p->values), x, y,
@@ -103,7 +100,32 @@ static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T
         default:
             MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "plan kernel %d not available", (int)v.kernel);
     }
-    if (h->opts.sync) MXS_CUDA(cudaStreamSynchronize(s));
+    return SPMV_SUCCESS;
+}
+template spmv_status_t plan_exec_stream<float>(spmv_plan_t, float, const float*, float, float*, cudaStream_t);
+template spmv_status_t plan_exec_stream<double>(spmv_plan_t, double, const double*, double, double*,
+                                                cudaStream_t);
+
+template <typename T>
+static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T* x, T beta, T* y) {
+    clear_error();
+    if (!h) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "handle is NULL");
+    MXS_TRY(plan_exec_stream<T>(p, alpha, x, beta, y, h->stream));
+    if (h->opts.sync) MXS_CUDA(cudaStreamSynchronize(h->stream));
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t plan_variant(spmv_handle_t* h, spmv_type_t type, int R, int C, int N, const int* rowPtr,
+                           const int* colIdx, const spmv_variant_t* variant, spmv_variant_t* out) {
+    *out = resolve(variant, R, N);
+    const HandleState* hs = static_cast<const HandleState*>(h->internal);
+    if ((!variant || variant->kernel == SPMV_KERNEL_AUTO) && hs && hs->selector && R > 0 && N > 0) {
+        std::vector<int> order;
+        MXS_TRY(learned_rank(hs->selector, type, R, C, N, rowPtr, colIdx, h->stream, order));
+        std::vector<spmv_variant_t> space(spmv_variant_space(nullptr, 0));
+        spmv_variant_space(space.data(), (int)space.size());
+        *out = resolve(&space[order[0]], R, N);
+    }
     return SPMV_SUCCESS;
 }
 
@@ -136,25 +158,23 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
     p->colIdx = colIdx;
     p->values = values;
     p->device = h->deviceId;
-    p->variant = resolve(variant, R, N);
-    const HandleState* hs = static_cast<const HandleState*>(h->internal);
-    if ((!variant || variant->kernel == SPMV_KERNEL_AUTO) && hs && hs->selector && R > 0 && N > 0) {
-        std::vector<int> order;
-        spmv_status_t sst = learned_rank(hs->selector, type, R, C, N, rowPtr, colIdx, h->stream, order);
+    {
+        const spmv_status_t sst = plan_variant(h, type, R, C, N, rowPtr, colIdx, variant, &p->variant);
         if (sst != SPMV_SUCCESS) {
             delete p;
             return sst;
         }
-        std::vector<spmv_variant_t> space(spmv_variant_space(nullptr, 0));
-        spmv_variant_space(space.data(), (int)space.size());
-        p->variant = resolve(&space[order[0]], R, N);
     }
     const size_t vs = type == SPMV_TYPE_FLOAT ? 4 : 8;
 
     spmv_status_t st = SPMV_SUCCESS;
     const spmv_variant_t& v = p->variant;
     if (v.kernel == SPMV_KERNEL_MERGE) {
-        const MergeGeom g = merge_geom_of(v);
+        MergeGeom g = merge_geom_of(v);
+        if (g.vec && N > 0 && !(aligned16(colIdx) && aligned16(values))) {
+            g = merge_unaligned_geom(g);
+            p->variant = spmv_variant_t{SPMV_KERNEL_MERGE, g.block, 0, g.ipt, 1};
+        }
         if (!merge_geom_supported(g)) {
             set_error(__FILE__, __LINE__, "unsupported merge shape block=%d ipt=%d", g.block, g.ipt);
             st = SPMV_ERROR_INTERNAL;
