@@ -213,9 +213,10 @@ typedef struct {
     spmv_kernel_t kernel;
     int blockSize;       /* threads per CTA: 128, 256 or 512               */
     int threadsPerRow;   /* VECTOR: 1,2,4,8,16,32; CSR5 with vectorWidth 32:
-                            tiles per chunk of a persistent launch (blocks
-                            of blockSize 256/512/1024 threads take chunks
-                            in turn), 0 = one tile per warp               */
+                            0 = one tile per warp; n > 0 = block ranges:
+                            a block of blockSize 256/512/1024 threads owns
+                            n tiles per warp of consecutive tiles, which
+                            its warps take one at a time                  */
     int itemsPerThread;  /* MERGE: merge items per thread (tile = block*ipt);
                             CSR5/BAND: nonzeros per lane (tile = 32*ipt)   */
     int vectorWidth;     /* VECTOR/MERGE: 1 or 4 elements per load;

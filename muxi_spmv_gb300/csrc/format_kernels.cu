@@ -164,7 +164,19 @@ spmv_status_t csr5_tile_bits(const int* rowPtr, int numRows, int sigma, long lon
     return SPMV_SUCCESS;
 }
 
-// sRp / sP: this warp's shared regions (kOrderedRpCap ints, 32E values).
+// Products go through shared memory from nonzero order (lane l holds
+// nonzeros l + 32e) to lane-contiguous order (lane l takes l*E .. l*E+E-1).
+// For E >= 8 nonzero j sits at slot j + j/32: the writes (fixed e,
+// consecutive lanes) and the reads (fixed e, lanes E apart; the pad makes
+// E*l + l/(32/E) cover every bank once) are both free of bank conflicts for
+// 4-byte values.  For E = 4 the unpadded layout is already conflict-free (a
+// lane's four values are one 16-byte read, eight lanes per 128 bytes).
+template <int E>
+__device__ __forceinline__ int ordered_slot(int j) {
+    return E >= 8 ? j + (j >> 5) : j;
+}
+
+// sRp / sP: this warp's shared regions (kOrderedRpCap ints, 33E values).
 // The rowPtr slice holds up to kOrderedRpCap entries (tiles spanning up to
 // 62 rows, nine in ten of the general tiles of a power-law matrix); a tile
 // over more rows reads rowPtr from global memory.  Small slices leave the
@@ -230,11 +242,11 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
 
     if (useBits) {
 #pragma unroll
-        for (int e = 0; e < E; ++e) sP[lane + 32 * e] = L.v[e] * g[e];
+        for (int e = 0; e < E; ++e) sP[ordered_slot<E>(lane + 32 * e)] = L.v[e] * g[e];
         __syncwarp();
         T p[E];
 #pragma unroll
-        for (int e = 0; e < E; ++e) p[e] = sP[lane * E + e];
+        for (int e = 0; e < E; ++e) p[e] = sP[ordered_slot<E>(lane * E + e)];
         csr5_tile_rows_bits<T, E>(p, L.bits, rFirst, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal);
         if (REUSE) __syncwarp();
         return;
@@ -249,11 +261,11 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
         }
     }
 #pragma unroll
-    for (int e = 0; e < E; ++e) sP[lane + 32 * e] = L.v[e] * g[e];
+    for (int e = 0; e < E; ++e) sP[ordered_slot<E>(lane + 32 * e)] = L.v[e] * g[e];
     __syncwarp();
     T p[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) p[e] = sP[lane * E + e];
+    for (int e = 0; e < E; ++e) p[e] = sP[ordered_slot<E>(lane * E + e)];
     csr5_tile_rows<T, E>(p, rFirst, rLast, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal,
                          [&](int r) { return (staged && r >= rFirst) ? sRp[r - rFirst] : __ldg(rowPtr + r); },
                          noEmpty);
@@ -286,7 +298,7 @@ csr5_ordered_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const 
                     T* __restrict__ carryVal, int noEmptyRows, const unsigned* __restrict__ tileBits) {
     constexpr int WARPS = BLOCK / 32;
     __shared__ int sRpAll[WARPS][kOrderedRpCap];
-    __shared__ __align__(16) T sPAll[WARPS][32 * E];
+    __shared__ __align__(16) T sPAll[WARPS][33 * E];
     const long long t = ((long long)blockIdx.x * BLOCK + threadIdx.x) >> 5;
     if (t >= tiles) return;  // uniform per warp
     const int w = threadIdx.x >> 5;
@@ -295,51 +307,40 @@ csr5_ordered_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const 
                             sPAll[w]);
 }
 
-// Persistent: block b takes chunks b, b + gridDim.x, ... of `chunk`
-// consecutive tiles, its WARPS warps taking a chunk's tiles in turn (the
-// warps of an SM work on neighbouring rows, so the near-diagonal x they gather
-// stays in that SM's L1).  Each warp loads its next tile while it computes
-// the current one.
-template <typename T, int E, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
-csr5_ordered_persistent_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int* __restrict__ colIdx,
-                               const T* __restrict__ values, const T* __restrict__ x, T* __restrict__ y, T alpha,
-                               T beta, int betaZero, const int* __restrict__ tileRow, long long tiles,
-                               int* __restrict__ carryRow, T* __restrict__ carryVal, int noEmptyRows, int chunk,
-                               const unsigned* __restrict__ tileBits) {
+// Block ranges: block b owns the `perBlock` consecutive tiles from
+// b*perBlock; its warps take them one at a time from a shared counter, so the
+// warps of a block work on neighbouring rows (the near-diagonal x they gather
+// stays in the SM's L1) and a warp that drew short tiles takes more of them
+// (no block waits for a slow tile while others idle, as one-tile-per-warp
+// launches of large blocks do).
+template <typename T, int E, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB)
+csr5_ordered_range_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int* __restrict__ colIdx,
+                          const T* __restrict__ values, const T* __restrict__ x, T* __restrict__ y, T alpha, T beta,
+                          int betaZero, const int* __restrict__ tileRow, long long tiles, int* __restrict__ carryRow,
+                          T* __restrict__ carryVal, int noEmptyRows, int perBlock,
+                          const unsigned* __restrict__ tileBits) {
+    constexpr int WARPS = BLOCK / 32;
     __shared__ int sRpAll[WARPS][kOrderedRpCap];
-    __shared__ __align__(16) T sPAll[WARPS][32 * E];
+    __shared__ __align__(16) T sPAll[WARPS][33 * E];
+    __shared__ int sNext, sEnd;  // next tile to hand out, end of the range (shared: fewer live registers)
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // Tile and chunk counts fit in int: plans cap nnz below 2^31.
-    const int ntiles = (int)tiles;
-    const int chunks = (ntiles + chunk - 1) / chunk;
-    // this warp's tiles: ch*chunk + w + i*WARPS inside chunk ch, for chunks
-    // ch = blockIdx.x, blockIdx.x + gridDim.x, ...
-    int ch = blockIdx.x, t = -1;
-    for (; ch < chunks; ch += gridDim.x) {
-        t = ch * chunk + w;
-        if (t < ntiles && t < ch * chunk + chunk) break;
-        t = -1;
+    // Tile counts fit in int: plans cap nnz below 2^31.
+    int t = blockIdx.x * perBlock + w;
+    if (threadIdx.x == 0) {
+        sNext = blockIdx.x * perBlock + WARPS;
+        sEnd = min(blockIdx.x * perBlock + perBlock, (int)tiles);
     }
-    if (t < 0) return;
-    OrderedLoad<T, E> cur, nxt;
-    csr5_ordered_load<T, E>(cur, t, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
-    while (t >= 0) {
-        int tn = t + WARPS, chn = ch;
-        if (tn >= ntiles || tn >= ch * chunk + chunk) {
-            tn = -1;
-            for (chn = ch + gridDim.x; chn < chunks; chn += gridDim.x) {
-                tn = chn * chunk + w;
-                if (tn < ntiles && tn < chn * chunk + chunk) break;
-                tn = -1;
-            }
-        }
-        if (tn >= 0) csr5_ordered_load<T, E>(nxt, tn, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
-        csr5_ordered_compute<T, E, true>(cur, t, lane, nnz, rowPtr, x, y, alpha, beta, betaZero != 0, tiles,
-                                         carryRow, carryVal, noEmptyRows != 0, sRpAll[w], sPAll[w], tileBits != nullptr);
-        cur = nxt;
-        t = tn;
-        ch = chn;
+    __syncthreads();
+    while (t < sEnd) {
+        OrderedLoad<T, E> L;
+        csr5_ordered_load<T, E>(L, t, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
+        int next = 0;  // drawn before the compute so its latency hides under the loads
+        if (lane == 0) next = atomicAdd(&sNext, 1);
+        csr5_ordered_compute<T, E, true>(L, t, lane, nnz, rowPtr, x, y, alpha, beta, betaZero != 0, tiles,
+                                         carryRow, carryVal, noEmptyRows != 0, sRpAll[w], sPAll[w],
+                                         tileBits != nullptr);
+        t = __shfl_sync(0xffffffffu, next, 0);
     }
 }
 
@@ -462,24 +463,6 @@ __global__ void csr5_fixup_kernel(long long tiles, const int* __restrict__ carry
     y[r] += alpha * s;
 }
 
-template <typename T, int E, int WARPS>
-static spmv_status_t launch_ordered_persistent(const int* tileRow, long long tiles, int* carryRow, T* carryVal,
-                                               const RowsArgs<T>& a, int chunk, const unsigned* bits, cudaStream_t s) {
-    static int perSM = -1;  // resident blocks per SM of this instantiation
-    if (perSM < 0) {
-        int n = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, csr5_ordered_persistent_kernel<T, E, WARPS>, WARPS * 32, 0);
-        perSM = n > 0 ? n : 1;
-    }
-    const long long chunks = (tiles + chunk - 1) / chunk;
-    long long g = (long long)current_sm_count() * perSM;
-    if (g > chunks) g = chunks;
-    csr5_ordered_persistent_kernel<T, E, WARPS><<<(unsigned)g, WARPS * 32, 0, s>>>(
-        a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha, a.beta, a.betaZero, tileRow, tiles,
-        carryRow, carryVal, a.noEmptyRows, chunk, bits);
-    return SPMV_SUCCESS;
-}
-
 template <typename T, int E>
 static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* carryRow, T* carryVal,
                                     const RowsArgs<T>& a, int block, int chunk, const unsigned* bits, cudaStream_t s) {
@@ -499,12 +482,22 @@ static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* ca
 #undef MXS_ORDERED
         return SPMV_SUCCESS;
     }
+    // Block ranges of `chunk` tiles per warp.
+    constexpr bool wide = E * sizeof(T) >= 64;
+    const long long per = (long long)chunk * (block / 32);
+    if (per > 0x7fffffffLL) MXS_FAIL(SPMV_ERROR_INTERNAL, "CSR5 block range too large");
+#define MXS_RANGE(B, M)                                                                                          \
+    csr5_ordered_range_kernel<T, E, B, M><<<grid_for(tiles, (int)per), B, 0, s>>>(                                \
+        a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha, a.beta, a.betaZero, tileRow, tiles,   \
+        carryRow, carryVal, a.noEmptyRows, (int)per, bits)
     switch (block) {
-        case 256: return launch_ordered_persistent<T, E, 8>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, s);
-        case 512: return launch_ordered_persistent<T, E, 16>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, s);
-        case 1024: return launch_ordered_persistent<T, E, 32>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, s);
-        default: MXS_FAIL(SPMV_ERROR_INTERNAL, "persistent CSR5 block must be 256, 512 or 1024 (got %d)", block);
+        case 256: MXS_RANGE(256, wide ? 3 : 8); break;
+        case 512: MXS_RANGE(512, wide ? 2 : 4); break;
+        case 1024: MXS_RANGE(1024, wide ? 1 : 2); break;
+        default: MXS_FAIL(SPMV_ERROR_INTERNAL, "block-range CSR5 block must be 256, 512 or 1024 (got %d)", block);
     }
+#undef MXS_RANGE
+    return SPMV_SUCCESS;
 }
 
 template <typename T>

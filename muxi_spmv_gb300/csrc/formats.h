@@ -24,8 +24,8 @@ spmv_status_t csr5_chains(const int* rowPtr, int numRows, int nnz, int sigma, co
 
 // Tile kernel then carry fix-up; carryRow/carryVal hold `tiles` entries.
 // ordered: gathers issued in nonzero order (csr5_ordered_kernel); with
-// chunk > 0 the ordered tiles run persistently, blocks of `block` threads
-// taking chunks of `chunk` consecutive tiles.
+// chunk > 0 each block of `block` threads owns chunk * block/32 consecutive
+// tiles that its warps take one at a time (csr5_ordered_range_kernel).
 template <typename T>
 spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
                        const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain = nullptr, bool ordered = false,

@@ -202,7 +202,7 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
             (v.threadsPerRow > 0 ? (v.blockSize != 256 && v.blockSize != 512 && v.blockSize != 1024)
                                  : (v.blockSize != 128 && v.blockSize != 256 && v.blockSize != 512 &&
                                     v.blockSize != 1024))) {
-            set_error(__FILE__, __LINE__, "ordered CSR5 needs blockSize 128/256/512/1024 (persistent 256/512/1024), got %d",
+            set_error(__FILE__, __LINE__, "ordered CSR5 needs blockSize 128/256/512/1024 (block ranges 256/512/1024), got %d",
                       v.blockSize);
             st = SPMV_ERROR_INTERNAL;
         } else if (v.kernel == SPMV_KERNEL_BAND && !band_shape_supported(v.blockSize, v.itemsPerThread)) {

@@ -99,15 +99,16 @@ PLAN_VARIANTS = [("band", 7, 256, 8, 4, 0), ("band", 7, 256, 4, 4, 0), ("band", 
                  ("band", 7, 512, 4, 4, 0), ("csr5_512", 4, 256, 16, 4, 0), ("csr5_128", 4, 256, 4, 4, 0),
                  ("csr5o_128", 4, 256, 4, 32, 0), ("csr5o_256", 4, 256, 8, 32, 0), ("csr5o_512", 4, 256, 16, 32, 0),
                  ("csr5o_b128", 4, 128, 8, 32, 0), ("csr5o_b512", 4, 512, 8, 32, 0), ("csr5o_b1024", 4, 1024, 8, 32, 0),
-                 ("csr5p_256c3", 4, 256, 8, 32, 3), ("csr5p_512c64", 4, 512, 4, 32, 64),
-                 ("csr5p_1024c32", 4, 1024, 8, 32, 32)]
+                 ("csr5r_256c3", 4, 256, 8, 32, 3), ("csr5r_512c64", 4, 512, 4, 32, 64),
+                 ("csr5r_1024c8", 4, 1024, 8, 32, 8), ("csr5r_1024c1", 4, 1024, 16, 32, 1)]
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
 @pytest.mark.parametrize("var", PLAN_VARIANTS, ids=[f"{v[0]}b{v[2]}e{v[3]}w{v[4]}" for v in PLAN_VARIANTS])
 def test_plan_variants_match_oracle(mx, cuda, handle, cases, var, dtype):
     """Plan-only kernels (tile metadata built at plan creation): the windowed
-    persistent kernel and CSR5 at every tile size, on every edge case."""
+    persistent kernel, CSR5 at every tile size and block shape, and CSR5
+    block ranges, on every edge case."""
     torch = cuda
     name_, kernel, block, ept, vw, tpr = var
     for name, (rp, ci, v, cols) in cases.items():
