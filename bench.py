@@ -192,6 +192,11 @@ def gpu_arm(args):
     if args.variant:
         k, b, t, i, w = (int(z) for z in args.variant.split(","))
         var = mx.make_variant(k, b, t, i, w)
+    model = None
+    if args.select == "learned" and not args.variant:
+        from muxi_spmv_gb300 import selector as S
+        model = S.MLP.load(S.DEFAULT_MODEL)
+        S.set_selector(h, model)  # AUTO plans take the learned pick
     perm = None
     if args.colperm != "none":
         # Column reorder on the GPU (reorderColumns / "RCM" / frequency orders),
@@ -306,6 +311,32 @@ def gpu_arm(args):
         if pipe_parity["rows_out_of_bound"]:
             print(f"PIPELINE PARITY FAILURE: {pipe_parity}", file=sys.stderr)
         pipe.destroy()
+    # ---- the vendor library on the same matrix and x: cuSPARSE SpMV through
+    # torch.sparse (context only; nothing of ours on this path).
+    vendor = None
+    if not args.no_vendor and perm is None:
+        import warnings
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            Acsr = torch.sparse_csr_tensor(A.d_rowPtr, A.d_colIdx[:A.nnz], A.d_values[:A.nnz],
+                                           size=(A.numRows, A.numCols), check_invariants=False)
+            with torch.cuda.stream(stream):
+                yv = torch.mv(Acsr, x)
+                for _ in range(args.warmup):
+                    torch.mv(Acsr, x)
+                h0 = torch.cuda.Event(enable_timing=True)
+                h1 = torch.cuda.Event(enable_timing=True)
+                h0.record(stream)
+                for _ in range(args.steps):
+                    torch.mv(Acsr, x)
+                h1.record(stream)
+            torch.cuda.synchronize(dev)
+        v_ms = h0.elapsed_time(h1) / args.steps
+        r = oracle.row_errors(yv.cpu().numpy(), y_ref, absum, 1e-5 if dtype == np.float32 else 1e-13)
+        vendor = {"library": "cuSPARSE SpMV via torch.sparse_csr_tensor / torch.mv (torch " + torch.__version__ + ")",
+                  "value": round(nbytes / (v_ms * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_step": round(v_ms, 5),
+                  "rows_out_of_bound": int((r > 1).sum())}
+        del Acsr
     clocks.stop()
 
     if ws > 1:
@@ -342,6 +373,7 @@ def gpu_arm(args):
             "config": {"workload": args.workload + (f"+colperm_{args.colperm}" if perm is not None else ""),
                        "rows": A.numRows, "cols": A.numCols, "nnz": A.nnz,
                        "distinct_cols": distinct, "algorithmic_bytes": int(nbytes), "variant": pv,
+                       "select": "explicit variant" if args.variant else args.select,
                        "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas{ws}",
                        "gflops": round(2 * A.nnz / (step_ms * 1e-3) / 1e9, 2), "generate_s": round(gen_s, 2)},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
@@ -358,7 +390,7 @@ def gpu_arm(args):
                     "pipeline_parity": pipe_parity},
             "gpu_launches": args.steps * launches_per_step * 2 +
                             (args.steps * pipe_info["launches_per_request"] if pipe_info else 0),
-            "clocks": clocks.summary(), "parity": parity}
+            "clocks": clocks.summary(), "parity": parity, "vendor_library": vendor}
 
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -605,6 +637,9 @@ def main():
     ap.add_argument("--variant", default="", help="kernel,block,tpr,ipt,vec (spmv_variant_t)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-pipeline", action="store_true", help="e2e through one stream, copies not overlapped")
+    ap.add_argument("--no-vendor", action="store_true", help="skip the cuSPARSE comparison")
+    ap.add_argument("--select", default="default", choices=["default", "learned"],
+                    help="AUTO plan: the fixed default variant, or the learned selector's pick")
     ap.add_argument("--slices", type=int, default=1, help="host pipeline row slices")
     ap.add_argument("--depth", type=int, default=2, help="host pipeline requests in flight")
     ap.add_argument("--scale-rows", type=int, default=0, help="same law on this many rows (profiling cases)")

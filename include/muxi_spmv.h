@@ -475,8 +475,9 @@ SPMV_API spmv_status_t spmv_gen_vector_f64(long long n, unsigned long long seed,
 /* Device-side generators for corpora and batches: same length laws as the
  * host generators for SPMV_GEN_POISSON_UNIFORM, SPMV_GEN_ZIPF_UNIFORM,
  * SPMV_GEN_BANDED and SPMV_GEN_BLOCKDIAG, drawn on the GPU (values differ
- * from the host generators').  Columns are sorted within a row and may
- * repeat where a row is dense in its range.  All pointers are device
+ * from the host generators'), and the host generators' SPMV_GEN_STENCIL2D
+ * and SPMV_GEN_STENCIL3D operators (3D values drawn here).  Columns are
+ * sorted within a row and may repeat where a row is dense in its range.  All pointers are device
  * pointers; spmv_gen_device_row_ptr synchronises the stream to read nnz and
  * fails with SPMV_ERROR_INVALID_MATRIX when nnz >= 2^31. */
 SPMV_API spmv_status_t spmv_gen_device_row_ptr(const spmv_gen_params_t* p, int* rowPtr, long long* nnz,

@@ -7,7 +7,8 @@
 // with E_0..E_k ~ Exp(1) and S = sum E, column i = lo + floor(range *
 // (E_0+..+E_i) / S).  Columns may repeat when a row is dense in its range
 // (CSR with repeated columns is well defined: the entries add).  Values are
-// N(0,1) (Box-Muller); x vectors U[lo,hi].  Each draw is a counter-based hash
+// N(0,1) (Box-Muller); x vectors U[lo,hi].  Stencil laws build the grid
+// operators directly.  Each draw is a counter-based hash
 // of (seed, row, element), so results do not depend on the launch shape.
 #include <vector>
 
@@ -118,6 +119,58 @@ __global__ void dgen_fill_kernel(DevLaw L, const int* __restrict__ rowPtr, int* 
     }
 }
 
+// Stencils (no length law): the 5-point Laplacian on an nx x ny grid (4 on
+// the diagonal, -1 off it) and the 27-point stencil on n0 x n1 x n2 (N(0,1)
+// values), columns ascending -- the host generator's matrices (the 3D values
+// come from this file's hash, so they differ from the host's).
+__device__ __forceinline__ bool dstencil(const DevLaw& L) {
+    return L.kind == SPMV_GEN_STENCIL2D || L.kind == SPMV_GEN_STENCIL3D;
+}
+__device__ __forceinline__ int dstencil_len(const DevLaw& L, long long r) {
+    if (L.kind == SPMV_GEN_STENCIL2D) {
+        const long long nx = (long long)L.p0, ny = (long long)L.p1, i = r / ny, j = r % ny;
+        return 1 + (i > 0) + (i < nx - 1) + (j > 0) + (j < ny - 1);
+    }
+    const long long n0 = (long long)L.p0, n1 = (long long)L.p1, n2 = (long long)L.p2;
+    const long long k = r / (n1 * n2), rem = r % (n1 * n2), j = rem / n2, i = rem % n2;
+    return (1 + (k > 0) + (k < n0 - 1)) * (1 + (j > 0) + (j < n1 - 1)) * (1 + (i > 0) + (i < n2 - 1));
+}
+
+__global__ void dgen_stencil_lengths_kernel(DevLaw L, unsigned* __restrict__ len) {
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < L.numRows) len[r] = (unsigned)dstencil_len(L, r);
+}
+
+template <typename T>
+__global__ void dgen_stencil_fill_kernel(DevLaw L, const int* __restrict__ rowPtr, int* __restrict__ colIdx,
+                                         T* __restrict__ values) {
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= L.numRows) return;
+    int n = rowPtr[r];
+    if (L.kind == SPMV_GEN_STENCIL2D) {
+        const long long nx = (long long)L.p0, ny = (long long)L.p1, i = r / ny, j = r % ny;
+        if (i > 0) { colIdx[n] = (int)(r - ny); values[n++] = T(-1); }
+        if (j > 0) { colIdx[n] = (int)(r - 1); values[n++] = T(-1); }
+        colIdx[n] = (int)r;
+        values[n++] = T(4);
+        if (j < ny - 1) { colIdx[n] = (int)(r + 1); values[n++] = T(-1); }
+        if (i < nx - 1) { colIdx[n] = (int)(r + ny); values[n++] = T(-1); }
+        return;
+    }
+    const long long n0 = (long long)L.p0, n1 = (long long)L.p1, n2 = (long long)L.p2;
+    const long long k = r / (n1 * n2), rem = r % (n1 * n2), j = rem / n2, i = rem % n2;
+    int e = 0;
+    for (int dk = -1; dk <= 1; ++dk)
+        for (int dj = -1; dj <= 1; ++dj)
+            for (int di = -1; di <= 1; ++di, ++e) {
+                const long long kk = k + dk, jj = j + dj, ii = i + di;
+                if (kk < 0 || kk >= n0 || jj < 0 || jj >= n1 || ii < 0 || ii >= n2) continue;
+                colIdx[n] = (int)((kk * n1 + jj) * n2 + ii);
+                const double u1 = dunif(L.seed, r, e, 2), u2 = dunif(L.seed, r, e, 3);
+                values[n++] = (T)(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
+            }
+}
+
 __global__ void sum64_kernel(long long n, const unsigned* __restrict__ v, unsigned long long* __restrict__ out) {
     unsigned long long s = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -134,8 +187,17 @@ __global__ void dgen_vector_kernel(long long n, unsigned long long seed, double 
 
 static bool device_law_ok(const spmv_gen_params_t* p) {
     if (!p || p->numRows < 0 || p->numCols <= 0) return false;
+    if (p->kind == SPMV_GEN_STENCIL2D)
+        return p->p0 >= 1 && p->p1 >= 1 && (long long)p->p0 * (long long)p->p1 == p->numRows &&
+               p->numRows == p->numCols;
+    if (p->kind == SPMV_GEN_STENCIL3D)
+        return p->p0 >= 1 && p->p1 >= 1 && p->p2 >= 1 &&
+               (long long)p->p0 * (long long)p->p1 * (long long)p->p2 == p->numRows && p->numRows == p->numCols;
     return p->kind == SPMV_GEN_POISSON_UNIFORM || p->kind == SPMV_GEN_ZIPF_UNIFORM || p->kind == SPMV_GEN_BANDED ||
            p->kind == SPMV_GEN_BLOCKDIAG;
+}
+static bool is_stencil(const spmv_gen_params_t* p) {
+    return p->kind == SPMV_GEN_STENCIL2D || p->kind == SPMV_GEN_STENCIL3D;
 }
 
 static DevLaw law_of(const spmv_gen_params_t* p) {
@@ -154,7 +216,10 @@ spmv_status_t spmv_gen_device_row_ptr(const spmv_gen_params_t* p, int* rowPtr, l
     if (!rowPtr || !nnz) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "NULL output");
     std::vector<double> cdf;
     int first = 0;
-    if (!gen_length_table(*p, cdf, first)) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "no length table for this law");
+    if (is_stencil(p))
+        cdf.assign(1, 1.0);  // unused
+    else if (!gen_length_table(*p, cdf, first))
+        MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "no length table for this law");
     const long long R = p->numRows;
     void* buf = nullptr;
     MXS_TRY(scratch_alloc(&buf, sizeof(double) * cdf.size() + sizeof(unsigned long long) + sizeof(unsigned) * (R + 2),
@@ -168,7 +233,10 @@ spmv_status_t spmv_gen_device_row_ptr(const spmv_gen_params_t* p, int* rowPtr, l
     cudaError_t e = cudaMemcpyAsync(dcdf, cdf.data(), sizeof(double) * cdf.size(), cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(sum, 0, sizeof(*sum), stream);
     if (e == cudaSuccess && R > 0) {
-        dgen_lengths_kernel<<<grid_for(R, 256), 256, 0, stream>>>(law_of(p), dcdf, (int)cdf.size(), first, len);
+        if (is_stencil(p))
+            dgen_stencil_lengths_kernel<<<grid_for(R, 256), 256, 0, stream>>>(law_of(p), len);
+        else
+            dgen_lengths_kernel<<<grid_for(R, 256), 256, 0, stream>>>(law_of(p), dcdf, (int)cdf.size(), first, len);
         const unsigned g = grid_for(R, 256);
         sum64_kernel<<<g < 4096u ? g : 4096u, 256, 0, stream>>>(R, len, sum);
         e = cudaGetLastError();
@@ -199,8 +267,12 @@ spmv_status_t spmv_gen_device_fill_f32(const spmv_gen_params_t* p, const int* ro
     if (!device_law_ok(p)) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "law not available on the device generator");
     if (p->numRows == 0) return SPMV_SUCCESS;
     if (!rowPtr || !colIdx || !values) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "NULL array");
-    dgen_fill_kernel<float><<<grid_for((long long)p->numRows * 32, 256), 256, 0, stream>>>(law_of(p), rowPtr, colIdx,
-                                                                                          values);
+    if (is_stencil(p))
+        dgen_stencil_fill_kernel<float><<<grid_for(p->numRows, 256), 256, 0, stream>>>(law_of(p), rowPtr, colIdx,
+                                                                                       values);
+    else
+        dgen_fill_kernel<float><<<grid_for((long long)p->numRows * 32, 256), 256, 0, stream>>>(law_of(p), rowPtr,
+                                                                                              colIdx, values);
     MXS_LAUNCH_CHECK();
     return SPMV_SUCCESS;
 }

@@ -56,7 +56,7 @@ class DeviceCSR:
 
 def gen_device(spec: GenSpec, stream=None) -> DeviceCSR:
     """Generates `spec` on the device (laws POISSON_UNIFORM, ZIPF_UNIFORM,
-    BANDED, BLOCKDIAG); values N(0,1), FP32."""
+    BANDED, BLOCKDIAG, STENCIL2D, STENCIL3D); FP32."""
     torch = _torch()
     p = spec.params()
     s = _stream_ptr(stream)

@@ -7,7 +7,8 @@
 corpus: seeded matrices generated on the GPU, one law per seed -- Poisson row
 lengths, Zipf lengths (s in [1.3, 2.5]), banded (width 3..1025) and
 block-diagonal (8..256 blocks) -- with rows log-uniform in [1e4, 1e7] and mean
-row length log-uniform in [2, 128], FP32 N(0,1) values.  Each matrix gets its
+row length log-uniform in [2, 128], FP32 N(0,1) values; seeds from
+STENCIL_SEED0 on are grid stencils (2D 5-point, 3D 27-point).  Each matrix gets its
 32 features (spmv_matrix_features) and the exhaustive autotuner's time for
 every variant of the space plus the reference heuristic's pick.  Records are
 written in chunks, so an interrupted run resumes where it stopped.
@@ -34,9 +35,13 @@ from pathlib import Path
 import numpy as np
 
 from . import api, selector
-from .api import GenSpec, GEN_BANDED, GEN_BLOCKDIAG, GEN_POISSON_UNIFORM, GEN_ZIPF_UNIFORM, Variant
+from .api import (GenSpec, GEN_BANDED, GEN_BLOCKDIAG, GEN_POISSON_UNIFORM, GEN_STENCIL2D, GEN_STENCIL3D,
+                  GEN_ZIPF_UNIFORM, Variant)
 
-LAWS = ("poisson", "zipf", "banded", "blockdiag")
+LAWS = ("poisson", "zipf", "banded", "blockdiag", "stencil")
+# Seeds from here on draw grid stencils (2D 5-point or 3D 27-point); below
+# it the law is LAWS[seed % 4].
+STENCIL_SEED0 = 1_000_000
 HEURISTIC_COL = -1  # last column of the label matrix: the heuristic's variant
 DEFAULT_VARIANT = Variant(api.KERNEL_CSR5, 128, 0, 8, 32)  # the AUTO plan without a model
 
@@ -53,6 +58,8 @@ def _zipf_clip_for_mean(s: float, target: float, cap: int) -> int:
 def spec_for_seed(seed: int, max_rows: int = 10_000_000, max_nnz: int = 600_000_000):
     """The corpus matrix of `seed`: (GenSpec, law name, target mean row length)."""
     rng = np.random.default_rng(np.random.SeedSequence([0x5E1EC7, seed]))
+    if seed >= STENCIL_SEED0:
+        return stencil_spec(rng, seed, max_rows)
     law = LAWS[seed % 4] if seed >= 0 else LAWS[0]
     lo = math.log10(1e4)
     R = int(round(10 ** rng.uniform(lo, math.log10(max_rows))))
@@ -75,6 +82,25 @@ def spec_for_seed(seed: int, max_rows: int = 10_000_000, max_nnz: int = 600_000_
         nb = int(rng.integers(8, 257))
         spec = GenSpec(GEN_BLOCKDIAG, R, C, float(nb), m, 0.0, 0.0, gseed)
     return spec, law, m
+
+
+def stencil_spec(rng, seed: int, max_rows: int):
+    """A 2D 5-point grid (rows log-uniform 1e4..max_rows, aspect 1..16) or a
+    3D 27-point grid (rows log-uniform 1e4..max_rows/4)."""
+    gseed = 1_000_003 * seed + 17
+    if rng.uniform() < 0.5:
+        R = 10 ** rng.uniform(4, math.log10(max_rows))
+        aspect = 2 ** rng.uniform(0, 4)
+        ny = max(2, int(round(math.sqrt(R * aspect))))
+        nx = max(2, int(round(R / ny)))
+        spec = GenSpec(GEN_STENCIL2D, nx * ny, nx * ny, float(nx), float(ny), 0.0, 0.0, gseed)
+        return spec, "stencil", 5.0
+    R = 10 ** rng.uniform(4, math.log10(max_rows / 4))
+    dims = [max(2, int(round(R ** (1 / 3) * 2 ** rng.uniform(-0.5, 0.5)))) for _ in range(2)]
+    n0 = max(2, int(round(R / (dims[0] * dims[1]))))
+    n = n0 * dims[0] * dims[1]
+    spec = GenSpec(GEN_STENCIL3D, n, n, float(n0), float(dims[0]), float(dims[1]), 0.0, gseed)
+    return spec, "stencil", 27.0
 
 
 def default_index() -> int:
@@ -137,12 +163,21 @@ def cmd_corpus(a):
             break
 
 
-def load_corpus(d) -> dict:
-    files = sorted(Path(d).glob("corpus_*.npz"))
+def load_corpus(spec: str) -> dict:
+    """Records of one or more corpora (comma-separated): chunk directories
+    written by `corpus`, or merged .npz files (save_corpus)."""
+    files = []
+    for d in str(spec).split(","):
+        p = Path(d)
+        files += [p] if p.is_file() else sorted(p.glob("corpus_*.npz"))
     if not files:
-        raise FileNotFoundError(f"no corpus chunks in {d}")
+        raise FileNotFoundError(f"no corpus records in {spec}")
     parts = [np.load(f) for f in files]
     return {k: np.concatenate([p[k] for p in parts]) for k in ("features", "ms", "meta")}
+
+
+def save_corpus(data: dict, path) -> None:
+    np.savez_compressed(path, **{k: data[k] for k in ("features", "ms", "meta")})
 
 
 def targets(ms_space: np.ndarray, clip: float = math.log(20.0)):
@@ -205,7 +240,10 @@ def cmd_train(a):
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     model.save(a.model)
+    if a.merged:
+        save_corpus(data, a.merged)
     rep = evaluate(model, data)
+    rep["by_law"] = evaluate_by_law(model, data)
     rep["train_seconds"] = train_s
     rep["train_steps"] = step
     print(json.dumps(rep, indent=1))
@@ -237,6 +275,19 @@ def evaluate(model, data, split_name: str = "test") -> dict:
             "autotune_seconds_median": float(np.median(data["meta"][sel, 6]))}
 
 
+def evaluate_by_law(model, data) -> dict:
+    """Held-out mean regret of the learned pick per generator law."""
+    import torch
+    ms = data["ms"][:, :HEURISTIC_COL]
+    _, te = split(data["meta"])
+    X = torch.from_numpy(data["features"][te].astype(np.float32)).cuda()
+    picks = learned_picks(model.forward(X).cpu().numpy(), ms[te])
+    r = regrets(picks, ms[te])
+    laws = data["meta"][te, 1].astype(int)
+    return {LAWS[k]: {"matrices": int((laws == k).sum()), "mean": float(r[laws == k].mean())}
+            for k in sorted(set(laws.tolist()))}
+
+
 def selection_cost(model, count: int = 8, max_rows: int = 2_000_000) -> dict:
     """Wall time of spmv_select(LEARNED) vs spmv_autotune on a few matrices."""
     import torch
@@ -264,7 +315,8 @@ def selection_cost(model, count: int = 8, max_rows: int = 2_000_000) -> dict:
 def cmd_evaluate(a):
     data = load_corpus(a.corpus)
     model = selector.MLP.load(a.model)
-    rep = {"test": evaluate(model, data, "test"), "train": evaluate(model, data, "train")}
+    rep = {"test": evaluate(model, data, "test"), "train": evaluate(model, data, "train"),
+           "by_law": evaluate_by_law(model, data)}
     if a.cost:
         rep["selection_cost"] = selection_cost(model)
     print(json.dumps(rep, indent=1))
@@ -292,6 +344,7 @@ def main(argv=None):
     t.add_argument("--lr", type=float, default=2e-3)
     t.add_argument("--seed", type=int, default=0)
     t.add_argument("--report")
+    t.add_argument("--merged", help="also write the combined records to this .npz")
     e = sub.add_parser("evaluate")
     e.add_argument("--corpus", required=True)
     e.add_argument("--model", required=True)

@@ -78,6 +78,26 @@ def test_device_generator_laws(mx, sel, cuda, law):
     assert not np.array_equal(host(A3.d_rowPtr), rp) or not np.array_equal(host(A3.d_colIdx)[:A3.nnz], ci)
 
 
+@pytest.mark.parametrize("kind", ["2d", "3d"])
+def test_device_stencils_match_host_generator(mx, sel, cuda, kind):
+    """Device stencil operators have the host generator's structure (and,
+    for the 5-point Laplacian, its values)."""
+    if kind == "2d":
+        spec = mx.GenSpec(mx.GEN_STENCIL2D, 37 * 53, 37 * 53, 37.0, 53.0, 0.0, 0.0, 4)
+    else:
+        spec = mx.GenSpec(mx.GEN_STENCIL3D, 9 * 11 * 7, 9 * 11 * 7, 9.0, 11.0, 7.0, 0.0, 4)
+    A = sel.gen_device(spec)
+    cuda.cuda.synchronize()
+    rp, ci, v = mx.generate(spec)
+    assert np.array_equal(host(A.d_rowPtr), rp)
+    assert np.array_equal(host(A.d_colIdx)[:A.nnz], ci)
+    dv = host(A.d_values)[:A.nnz]
+    if kind == "2d":
+        assert np.array_equal(dv, v)
+    else:
+        assert abs(dv.astype(np.float64).mean()) < 0.1 and abs(dv.std() - 1.0) < 0.1
+
+
 def test_device_generator_values_and_vector(mx, sel, cuda):
     _, A = _gen(mx, sel, mx.GEN_POISSON_UNIFORM, 20000, 30.0, 1.0, 80.0, seed=3)
     v = host(A.d_values)[:A.nnz].astype(np.float64)
