@@ -239,7 +239,6 @@ def gpu_arm(args):
     time.sleep(0.3)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    plan.profile(True)
     torch.cuda.synchronize(dev)
     e0.record(stream)
     for _ in range(args.steps):
@@ -247,6 +246,12 @@ def gpu_arm(args):
     e1.record(stream)
     torch.cuda.synchronize(dev)
     step_ms = e0.elapsed_time(e1) / args.steps
+    # The main kernel alone: the plan records an event pair around it (a
+    # separate pass, since an event between the tile kernel and its fix-up
+    # keeps the fix-up from launching behind the tile kernel's last wave).
+    plan.profile(True)
+    for _ in range(args.steps):
+        plan.exec(x, y)
     kern_ms_total, kern_launches = plan.profile_read()
     plan.profile(False)
 
@@ -388,7 +393,7 @@ def gpu_arm(args):
                     "serial": {"value": round(serial_val, 3), "ms_per_step": round(serial_ms, 5),
                                "call": "H2D(x), spmv_plan_exec, D2H(y) in order on one stream"},
                     "pipeline_parity": pipe_parity},
-            "gpu_launches": args.steps * launches_per_step * 2 +
+            "gpu_launches": args.steps * launches_per_step * 3 +
                             (args.steps * pipe_info["launches_per_request"] if pipe_info else 0),
             "clocks": clocks.summary(), "parity": parity, "vendor_library": vendor}
 

@@ -52,6 +52,14 @@ __device__ __forceinline__ double2 ld_stream2(const double* p) {
 template <typename T>
 __device__ __forceinline__ T ld_x(const T* p) { return __ldg(p); }
 
+// Programmatic dependent launch: a kernel calls pdl_trigger() to let the
+// next kernel of its stream (launched with programmatic stream
+// serialization) be scheduled early; that kernel's pdl_wait() returns once
+// the triggering grid has completed and its writes are visible.  Without the
+// launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Four consecutive values as an array (float: one 16-byte load; double: two).
 template <typename T> struct Quad { T v[4]; };
 __device__ __forceinline__ Quad<float> ld_stream_quad(const float* p) {

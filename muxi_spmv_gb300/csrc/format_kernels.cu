@@ -299,6 +299,7 @@ csr5_ordered_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const 
     constexpr int WARPS = BLOCK / 32;
     __shared__ int sRpAll[WARPS][kOrderedRpCap];
     __shared__ __align__(16) T sPAll[WARPS][33 * E];
+    pdl_trigger();  // the carry fix-up may be scheduled behind the last wave
     const long long t = ((long long)blockIdx.x * BLOCK + threadIdx.x) >> 5;
     if (t >= tiles) return;  // uniform per warp
     const int w = threadIdx.x >> 5;
@@ -324,6 +325,7 @@ csr5_ordered_range_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, 
     __shared__ int sRpAll[WARPS][kOrderedRpCap];
     __shared__ __align__(16) T sPAll[WARPS][33 * E];
     __shared__ int sNext, sEnd;  // next tile to hand out, end of the range (shared: fewer live registers)
+    pdl_trigger();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // Tile counts fit in int: plans cap nnz below 2^31.
     int t = blockIdx.x * perBlock + w;
@@ -436,17 +438,46 @@ spmv_status_t csr5_chains(const int* rowPtr, int numRows, int nnz, int sigma, co
     return SPMV_SUCCESS;
 }
 
-// Adds each chain's carries in tile order.
+// Adds each chain's carries to its row.  A thread sums a chain of up to
+// kShortChain tiles in tile order; a longer chain (a row over more tiles) is
+// queued in shared memory and summed by a whole warp: lane-strided partial
+// sums, then the butterfly of group_sum.  Which warp takes a queued chain
+// varies, but each chain's order of additions is fixed, so results are
+// identical run to run -- and one 65,536-nonzero row no longer makes a single
+// thread walk 256 carries while the rest of the GPU idles.
+constexpr int kShortChain = 8;
 template <typename T>
-__global__ void csr5_chain_fixup_kernel(long long chains, const int* __restrict__ start, const int* __restrict__ end,
-                                        const int* __restrict__ row, const T* __restrict__ carryVal, T* __restrict__ y,
-                                        T alpha) {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= chains) return;
-    const int e = end[c];
-    T s = T(0);
-    for (int u = start[c]; u <= e; ++u) s += carryVal[u];
-    y[row[c]] += alpha * s;
+__global__ void __launch_bounds__(256)
+csr5_chain_fixup_kernel(long long chains, const int* __restrict__ start, const int* __restrict__ end,
+                        const int* __restrict__ row, const T* __restrict__ carryVal, T* __restrict__ y, T alpha) {
+    __shared__ int sLong[256];
+    __shared__ int sCount;
+    pdl_wait();  // the tile kernel's carries and y are complete
+    if (threadIdx.x == 0) sCount = 0;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * 256;
+    const long long c = base + threadIdx.x;
+    if (c < chains) {
+        const int b = start[c], e = end[c];
+        if (e - b < kShortChain) {
+            T s = T(0);
+#pragma unroll 4
+            for (int u = b; u <= e; ++u) s += carryVal[u];
+            y[row[c]] += alpha * s;
+        } else {
+            sLong[atomicAdd(&sCount, 1)] = threadIdx.x;
+        }
+    }
+    __syncthreads();
+    const int n = sCount, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x >> 5; i < n; i += 8) {
+        const long long cc = base + sLong[i];
+        const int b = start[cc], e = end[cc];
+        T s = T(0);
+        for (int u = b + lane; u <= e; u += 32) s += carryVal[u];
+        s = group_sum<32>(s);
+        if (lane == 0) y[row[cc]] += alpha * s;
+    }
 }
 
 // Adds each split row's carries in tile order (rows with carry -1 skipped).
@@ -537,9 +568,21 @@ spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carr
     if (afterMain) MXS_CUDA(cudaEventRecord(afterMain, s));
     if (chains && chains->n >= 0) {
         if (chains->n > 0) {
-            csr5_chain_fixup_kernel<T><<<grid_for(chains->n, 256), 256, 0, s>>>(
-                chains->n, chains->start, chains->end, chains->row, carryVal, a.y, a.alpha);
-            MXS_LAUNCH_CHECK();
+            // Right behind an ordered tile kernel (no event between them) the
+            // fix-up launches programmatically: its blocks are scheduled while
+            // the tile kernel's last wave runs and start when it completes.
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(grid_for(chains->n, 256));
+            cfg.blockDim = dim3(256);
+            cfg.stream = s;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = (ordered && !afterMain) ? 1 : 0;
+            MXS_CUDA(cudaLaunchKernelEx(&cfg, csr5_chain_fixup_kernel<T>, (long long)chains->n,
+                                        (const int*)chains->start, (const int*)chains->end, (const int*)chains->row,
+                                        (const T*)carryVal, a.y, a.alpha));
         }
         return SPMV_SUCCESS;
     }
