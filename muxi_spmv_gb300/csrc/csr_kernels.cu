@@ -43,9 +43,12 @@ csr_rows_kernel(int numRows, int nnz, const int* __restrict__ rowPtr,
                 const Quad<T> v = ld_stream_quad(values + q);
                 const int cc[4] = {c.x, c.y, c.z, c.w};
                 T part = T(0);
+                T g[4];  // every quad column is a valid index (q + 4 <= nnz)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) g[e] = ld_x(x + cc[e]);
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
-                    if (q + e >= js && q + e < je) part += v.v[e] * ld_x(x + cc[e]);
+                    if (q + e >= js && q + e < je) part += v.v[e] * g[e];
                 sum += part;
             } else {
                 // Last partial quad of the arrays: element loads, never past nnz.

@@ -11,46 +11,96 @@ namespace mxs {
 constexpr unsigned kFull = 0xffffffffu;
 
 // ---------------------------------------------------------------------------
+// L2 residency of x.  The matrix streams through L2 once per SpMV while x is
+// gathered over and over.  With MXS_L2_HINTS=1 every x gather carries an L2
+// evict_last policy and every matrix load an evict_first one (an access
+// window per instruction, no device-wide L2 set-aside).  Measured on GB300,
+// x stays in L2 without it (DRAM bytes of a power-law SpMV equal the
+// algorithmic bytes) and the hinted loads run 0.2-1.2% slower, so the
+// default is plain loads.
+// ---------------------------------------------------------------------------
+#ifndef MXS_L2_HINTS
+#define MXS_L2_HINTS 0
+#endif
+#if MXS_L2_HINTS
+#define MXS_STREAM_LD(TY, EXTRA) "ld.global.nc.L1::no_allocate.L2::cache_hint" TY " " EXTRA
+#define MXS_X_LD(TY) "ld.global.nc.L2::cache_hint" TY " %0, [%1], %2;"
+#else
+#define MXS_STREAM_LD(TY, EXTRA) "ld.global.nc.L1::no_allocate" TY " " EXTRA
+#define MXS_X_LD(TY) "ld.global.nc" TY " %0, [%1];"
+#endif
+__device__ __forceinline__ unsigned long long l2_evict_first() {
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ unsigned long long l2_evict_last() {
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// ---------------------------------------------------------------------------
 // Streaming loads for matrix data (read once per SpMV): no L1 allocation, so
 // the L1 keeps the x lines that neighbouring rows re-gather.
 // ---------------------------------------------------------------------------
+#if MXS_L2_HINTS
+#define MXS_POL , "l"(l2_evict_first())
+#define MXS_XPOL , "l"(l2_evict_last())
+#define MXS_P1 ", %2"
+#define MXS_P5 ", %5"
+#define MXS_P3 ", %3"
+#else
+#define MXS_POL
+#define MXS_XPOL
+#define MXS_P1 ""
+#define MXS_P5 ""
+#define MXS_P3 ""
+#endif
 __device__ __forceinline__ int ld_stream(const int* p) {
     int r;
-    asm("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(r) : "l"(p));
+    asm(MXS_STREAM_LD(".s32", "%0, [%1]" MXS_P1 ";") : "=r"(r) : "l"(p) MXS_POL);
     return r;
 }
 __device__ __forceinline__ float ld_stream(const float* p) {
     float r;
-    asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(r) : "l"(p));
+    asm(MXS_STREAM_LD(".f32", "%0, [%1]" MXS_P1 ";") : "=f"(r) : "l"(p) MXS_POL);
     return r;
 }
 __device__ __forceinline__ double ld_stream(const double* p) {
     double r;
-    asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(r) : "l"(p));
+    asm(MXS_STREAM_LD(".f64", "%0, [%1]" MXS_P1 ";") : "=d"(r) : "l"(p) MXS_POL);
     return r;
 }
 __device__ __forceinline__ int4 ld_stream4(const int* p) {
     int4 r;
-    asm("ld.global.nc.L1::no_allocate.v4.s32 {%0,%1,%2,%3}, [%4];"
-        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p));
+    asm(MXS_STREAM_LD(".v4.s32", "{%0,%1,%2,%3}, [%4]" MXS_P5 ";")
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p) MXS_POL);
     return r;
 }
 __device__ __forceinline__ float4 ld_stream4(const float* p) {
     float4 r;
-    asm("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
-        : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p));
+    asm(MXS_STREAM_LD(".v4.f32", "{%0,%1,%2,%3}, [%4]" MXS_P5 ";")
+        : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w) : "l"(p) MXS_POL);
     return r;
 }
 __device__ __forceinline__ double2 ld_stream2(const double* p) {
     double2 r;
-    asm("ld.global.nc.L1::no_allocate.v2.f64 {%0,%1}, [%2];"
-        : "=d"(r.x), "=d"(r.y) : "l"(p));
+    asm(MXS_STREAM_LD(".v2.f64", "{%0,%1}, [%2]" MXS_P3 ";") : "=d"(r.x), "=d"(r.y) : "l"(p) MXS_POL);
     return r;
 }
 
 // Gather of x: read-only path, L1 allocating.
-template <typename T>
-__device__ __forceinline__ T ld_x(const T* p) { return __ldg(p); }
+__device__ __forceinline__ float ld_x(const float* p) {
+    float r;
+    asm(MXS_X_LD(".f32") : "=f"(r) : "l"(p) MXS_XPOL);
+    return r;
+}
+__device__ __forceinline__ double ld_x(const double* p) {
+    double r;
+    asm(MXS_X_LD(".f64") : "=d"(r) : "l"(p) MXS_XPOL);
+    return r;
+}
 
 // Programmatic dependent launch: a kernel calls pdl_trigger() to let the
 // next kernel of its stream (launched with programmatic stream

@@ -627,14 +627,20 @@ ell_kernel(int numRows, int width, const int* __restrict__ ellCol, const T* __re
             c[u] = ld_stream(ellCol + idx);
             v[u] = ld_stream(ellVal + idx);
         }
+        // Padding (col -1) gathers x[0] and discards it: unconditional
+        // gathers keep the four loads in flight together.
+        T g[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (c[u] >= 0) sum += v[u] * ld_x(x + c[u]);
+        for (int u = 0; u < 4; ++u) g[u] = ld_x(x + (c[u] >= 0 ? c[u] : 0));
+#pragma unroll
+        for (int u = 0; u < 4; ++u) sum += c[u] >= 0 ? v[u] * g[u] : T(0);
     }
     for (; i < width; ++i) {
         const long long idx = r + (long long)i * numRows;
         const int c = ld_stream(ellCol + idx);
-        if (c >= 0) sum += ld_stream(ellVal + idx) * ld_x(x + c);
+        const T v = ld_stream(ellVal + idx);
+        const T g = ld_x(x + (c >= 0 ? c : 0));
+        sum += c >= 0 ? v * g : T(0);
     }
     y[r] = axpby(alpha, sum, beta, betaZero != 0, y + r);
 }

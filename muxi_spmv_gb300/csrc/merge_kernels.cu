@@ -172,10 +172,13 @@ merge_tile_kernel(int numRows, const int* __restrict__ rowPtr, const int* __rest
         }
         if (k < nr) sEnd[k] = __ldg(rowPtr + r0 + 1 + k);
     }
+    T g[IPT];
+#pragma unroll
+    for (int u = 0; u < IPT; ++u) g[u] = ld_x(x + (tid + u * BLOCK < nj ? cl[u] : 0));
 #pragma unroll
     for (int u = 0; u < IPT; ++u) {
         const int k = tid + u * BLOCK;
-        if (k < nj) sProd[k] = vl[u] * ld_x(x + cl[u]);
+        if (k < nj) sProd[k] = vl[u] * g[u];
     }
     __syncthreads();
 
@@ -277,10 +280,13 @@ __device__ __forceinline__ void load_span(const int* __restrict__ colIdx, const 
             const int4 c = ld_stream4(colIdx + base + q);
             const Quad<T> v = ld_stream_quad(values + base + q);
             const int cc[4] = {c.x, c.y, c.z, c.w};
+            T g[4];  // every quad column is a valid index (base + EPT <= nnz)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) g[e] = ld_x(x + cc[e]);
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 const int j = base + q + e;
-                p[q + e] = (j >= lo && j < hi) ? v.v[e] * ld_x(x + cc[e]) : T(0);
+                p[q + e] = (j >= lo && j < hi) ? v.v[e] * g[e] : T(0);
             }
         }
     } else {
