@@ -144,9 +144,10 @@ SPMV_API int spmv_abi_version(void);
 /* declared spmv_csr.cuh:1100-1106) and spmv_csr_exec<T>                */
 /* (src/api/spmv_api.h:82-92).  Unlike the reference, alpha and beta    */
 /* are applied; beta == 0 never reads y.  nnz == 0 still writes         */
-/* y = beta*y.  The call is stateless: it runs the load-balanced         */
-/* merge-path kernel and takes its scratch from the stream-ordered      */
-/* allocator of the call's stream.                                      */
+/* y = beta*y.  The call is stateless: it finds CSR5 tiles of 256       */
+/* nonzeros for this call, runs the ordered tile kernel and the carry    */
+/* fix-up (merge-path tiles beyond 2^31 - 32769 nonzeros), and takes its */
+/* scratch from the stream-ordered allocator of the call's stream.      */
 /* ------------------------------------------------------------------ */
 SPMV_API spmv_status_t spmv_csr_f32(int numRows, int numCols, int nnz,
                            const int* rowPtr, const int* colIdx, const float* values,

@@ -142,6 +142,26 @@ spmv_status_t merge_stateless(const MergeGeom& g, const RowsArgs<T>& a, cudaStre
     return st != SPMV_SUCCESS ? st : st2;
 }
 
+// The default stateless SpMV: CSR5 tiles of 256 nonzeros found for this call
+// (one binary search per tile), the ordered tile kernel (128-thread blocks)
+// and the tile-walking carry fix-up, all in stream-ordered scratch.
+template <typename T>
+spmv_status_t csr5_stateless(const RowsArgs<T>& a, cudaStream_t s) {
+    constexpr int kSigma = 256;
+    const long long tiles = ((long long)a.nnz + kSigma - 1) / kSigma;
+    const size_t a4 = ((sizeof(int) * tiles) + 255) & ~size_t(255);
+    void* buf = nullptr;
+    MXS_TRY(scratch_alloc(&buf, 2 * a4 + sizeof(T) * tiles, s));
+    int* tileRow = static_cast<int*>(buf);
+    int* carryRow = reinterpret_cast<int*>(static_cast<char*>(buf) + a4);
+    T* carryVal = reinterpret_cast<T*>(static_cast<char*>(buf) + 2 * a4);
+    spmv_status_t st = csr5_tiles(a.rowPtr, a.numRows, a.nnz, kSigma, tileRow, nullptr, s);
+    if (st == SPMV_SUCCESS)
+        st = run_csr5<T>(kSigma, tileRow, tiles, carryRow, carryVal, a, s, nullptr, true, 128, 0, nullptr, nullptr);
+    const spmv_status_t st2 = scratch_free(buf, s);
+    return st != SPMV_SUCCESS ? st : st2;
+}
+
 template <typename T>
 static spmv_status_t finish(const spmv_opts_t* opts, cudaStream_t s) {
     if (opts && opts->sync) MXS_CUDA(cudaStreamSynchronize(s));
@@ -202,6 +222,10 @@ static spmv_status_t csr_exec(const spmv_variant_t* v, int R, int C, int N, cons
         return finish<T>(opts, s);
     }
     RowsArgs<T> a{R, N, rowPtr, colIdx, values, x, y, alpha, beta, beta == T(0)};
+    if ((!v || v->kernel == SPMV_KERNEL_AUTO) && N <= 0x7fffffff - 32768) {
+        MXS_TRY(csr5_stateless<T>(a, s));
+        return finish<T>(opts, s);
+    }
     spmv_variant_t def{SPMV_KERNEL_MERGE, 256, 0, 8, 4};
     if (!v) v = &def;
     switch (v->kernel) {

@@ -480,18 +480,49 @@ csr5_chain_fixup_kernel(long long chains, const int* __restrict__ start, const i
     }
 }
 
-// Adds each split row's carries in tile order (rows with carry -1 skipped).
+// Adds each split row's carries (rows with carry -1 skipped), for callers
+// without a chain table: the thread at the first tile of a run of equal
+// carry rows walks it.  Runs of up to kShortChain tiles are summed in tile
+// order by that thread; longer ones go to a warp exactly as in
+// csr5_chain_fixup_kernel (same additions, so both fix-ups give the same bits).
 template <typename T>
-__global__ void csr5_fixup_kernel(long long tiles, const int* __restrict__ carryRow, const T* __restrict__ carryVal,
-                                  T* __restrict__ y, T alpha) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= tiles) return;
-    const int r = carryRow[t];
-    if (r < 0) return;
-    if (t > 0 && carryRow[t - 1] == r) return;
-    T s = T(0);
-    for (long long u = t; u < tiles && carryRow[u] == r; ++u) s += carryVal[u];
-    y[r] += alpha * s;
+__global__ void __launch_bounds__(256)
+csr5_fixup_kernel(long long tiles, const int* __restrict__ carryRow, const T* __restrict__ carryVal,
+                  T* __restrict__ y, T alpha) {
+    __shared__ int sLong[256];
+    __shared__ int sCount;
+    pdl_wait();
+    if (threadIdx.x == 0) sCount = 0;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * 256;
+    const long long t = base + threadIdx.x;
+    if (t < tiles) {
+        const int r = carryRow[t];
+        if (r >= 0 && (t == 0 || carryRow[t - 1] != r)) {
+            T s = T(0);
+            long long u = t;
+            for (; u < tiles && u - t < kShortChain && carryRow[u] == r; ++u) s += carryVal[u];
+            if (u - t == kShortChain && u < tiles && carryRow[u] == r)
+                sLong[atomicAdd(&sCount, 1)] = threadIdx.x;
+            else
+                y[r] += alpha * s;
+        }
+    }
+    __syncthreads();
+    const int n = sCount, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x >> 5; i < n; i += 8) {
+        const long long t0 = base + sLong[i];
+        const int r = carryRow[t0];
+        T s = T(0);
+        for (long long b = t0;; b += 32) {  // the run is contiguous: its lanes form a prefix
+            const long long u = b + lane;
+            const bool in = u < tiles && carryRow[u] == r;
+            if (in) s += carryVal[u];
+            if (!__all_sync(kFull, in)) break;
+        }
+        s = group_sum<32>(s);
+        if (lane == 0) y[r] += alpha * s;
+    }
 }
 
 template <typename T, int E>
@@ -566,27 +597,30 @@ spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carr
     }
     MXS_LAUNCH_CHECK();
     if (afterMain) MXS_CUDA(cudaEventRecord(afterMain, s));
+    // Right behind an ordered tile kernel (no event between them) the fix-up
+    // launches programmatically: its blocks are scheduled while the tile
+    // kernel's last wave runs and start when it completes.
+    cudaLaunchConfig_t cfg = {};
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = (ordered && !afterMain) ? 1 : 0;
     if (chains && chains->n >= 0) {
         if (chains->n > 0) {
-            // Right behind an ordered tile kernel (no event between them) the
-            // fix-up launches programmatically: its blocks are scheduled while
-            // the tile kernel's last wave runs and start when it completes.
-            cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(grid_for(chains->n, 256));
-            cfg.blockDim = dim3(256);
-            cfg.stream = s;
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-            attr[0].val.programmaticStreamSerializationAllowed = 1;
-            cfg.attrs = attr;
-            cfg.numAttrs = (ordered && !afterMain) ? 1 : 0;
             MXS_CUDA(cudaLaunchKernelEx(&cfg, csr5_chain_fixup_kernel<T>, (long long)chains->n,
                                         (const int*)chains->start, (const int*)chains->end, (const int*)chains->row,
                                         (const T*)carryVal, a.y, a.alpha));
         }
         return SPMV_SUCCESS;
     }
-    return run_csr5_fixup<T>(tiles, carryRow, carryVal, a, s);
+    cfg.gridDim = dim3(grid_for(tiles, 256));
+    MXS_CUDA(cudaLaunchKernelEx(&cfg, csr5_fixup_kernel<T>, tiles, (const int*)carryRow, (const T*)carryVal, a.y,
+                                a.alpha));
+    return SPMV_SUCCESS;
 }
 
 template <typename T>

@@ -31,7 +31,8 @@ static spmv_status_t csr5_exec(int R, int C, int N, const int* rowPtr, const int
         int* cr = static_cast<int*>(buf);
         T* cv = reinterpret_cast<T*>(static_cast<char*>(buf) + ((sizeof(int) * tiles + 255) & ~size_t(255)));
         RowsArgs<T> a{R, N, rowPtr, colIdx, values, x, y, alpha, beta, beta == T(0)};
-        spmv_status_t st = run_csr5<T>(sigma, tileRow, tiles, cr, cv, a, s);
+        // Gathers in nonzero order (the ordered tile kernel, 128-thread blocks).
+        spmv_status_t st = run_csr5<T>(sigma, tileRow, tiles, cr, cv, a, s, nullptr, true, 128);
         scratch_free(buf, s);
         MXS_TRY(st);
     }

@@ -28,7 +28,7 @@ __global__ void csr5_tiles_kernel(const int* __restrict__ rowPtr, int numRows, i
     const long long start = t * sigma;
     const int r = row_of_nnz(rowPtr, numRows, start);
     tileRow[t] = r;
-    tileOff[t] = (int)(start - rowPtr[r]);
+    if (tileOff) tileOff[t] = (int)(start - rowPtr[r]);
 }
 
 spmv_status_t csr5_tiles(const int* rowPtr, int numRows, int nnz, int sigma, int* tileRow, int* tileOff,
@@ -37,7 +37,7 @@ spmv_status_t csr5_tiles(const int* rowPtr, int numRows, int nnz, int sigma, int
     const long long tiles = ((long long)nnz + sigma - 1) / sigma;
     if (tiles == 0) return SPMV_SUCCESS;
     if (!rowPtr || numRows <= 0) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "rowPtr is NULL or no rows");
-    if (!tileRow || !tileOff) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "tile arrays are NULL");
+    if (!tileRow) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "tile row array is NULL");  // tileOff may be NULL
     csr5_tiles_kernel<<<grid_for(tiles, 256), 256, 0, s>>>(rowPtr, numRows, sigma, tiles, tileRow, tileOff);
     MXS_LAUNCH_CHECK();
     return SPMV_SUCCESS;
