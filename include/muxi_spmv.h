@@ -173,6 +173,25 @@ SPMV_API spmv_status_t spmv_csr_transpose_f64(int numRows, int numCols, int nnz,
                                               const int* colIdx, const double* values, int* tRowPtr, int* tColIdx,
                                               double* tValues, cudaStream_t stream);
 
+/* COO (src/formats/sparse_formats.h:113-162, COOMatrix: declared there
+ * without a kernel).  spmv_coo_to_csr_* orders the entries by (row, column);
+ * entries with equal (row, column) stay separate, in input order, and add.
+ * Entries outside the matrix are refused with SPMV_ERROR_INVALID_MATRIX (the
+ * check synchronises the stream).  spmv_coo_* converts in stream-ordered
+ * scratch and runs the stateless CSR SpMV. */
+SPMV_API spmv_status_t spmv_coo_to_csr_f32(int numRows, int numCols, int nnz, const int* rowIdx, const int* colIdx,
+                                           const float* values, int* rowPtr, int* outColIdx, float* outValues,
+                                           cudaStream_t stream);
+SPMV_API spmv_status_t spmv_coo_to_csr_f64(int numRows, int numCols, int nnz, const int* rowIdx, const int* colIdx,
+                                           const double* values, int* rowPtr, int* outColIdx, double* outValues,
+                                           cudaStream_t stream);
+SPMV_API spmv_status_t spmv_coo_f32(int numRows, int numCols, int nnz, const int* rowIdx, const int* colIdx,
+                                    const float* values, const float* x, float* y, float alpha, float beta,
+                                    const spmv_opts_t* opts);
+SPMV_API spmv_status_t spmv_coo_f64(int numRows, int numCols, int nnz, const int* rowIdx, const int* colIdx,
+                                    const double* values, const double* x, double* y, double alpha, double beta,
+                                    const spmv_opts_t* opts);
+
 /* FP32 CSR SpMV that allocates no device memory (no counterpart in the
  * reference).  Same kernels and results as spmv_csr_f32 (default merge-path
  * variant), for callers that cannot allocate: code recording a CUDA graph,

@@ -168,6 +168,92 @@ struct CSR5Matrix {
     }
 };
 
+// COOMatrix<T> (sparse_formats.h:113-162): the reference declares the type
+// without a kernel; here spmv_exec(SPMV_FORMAT_COO, ...) converts it to CSR
+// on the device and runs the stateless CSR SpMV.
+template <typename FloatType>
+struct COOMatrix {
+    int numRows = 0, numCols = 0, nnz = 0;
+    int* rowIdx = nullptr;
+    int* colIdx = nullptr;
+    FloatType* values = nullptr;
+    int* d_rowIdx = nullptr;
+    int* d_colIdx = nullptr;
+    FloatType* d_values = nullptr;
+    bool ownsHostMemory = false;
+    bool ownsDeviceMemory = false;
+
+    COOMatrix() = default;
+    COOMatrix(const COOMatrix&) = delete;
+    COOMatrix& operator=(const COOMatrix&) = delete;
+    ~COOMatrix() {
+        if (ownsHostMemory) {
+            std::free(rowIdx);
+            std::free(colIdx);
+            std::free(values);
+        }
+        if (ownsDeviceMemory) {
+            cudaFree(d_rowIdx);
+            cudaFree(d_colIdx);
+            cudaFree(d_values);
+        }
+    }
+    void allocateHost(int rows, int cols, int nonzeros) {
+        numRows = rows;
+        numCols = cols;
+        nnz = nonzeros;
+        const size_t n = (size_t)(nonzeros > 0 ? nonzeros : 1);
+        rowIdx = static_cast<int*>(std::malloc(sizeof(int) * n));
+        colIdx = static_cast<int*>(std::malloc(sizeof(int) * n));
+        values = static_cast<FloatType*>(std::malloc(sizeof(FloatType) * n));
+        ownsHostMemory = true;
+    }
+    void allocateDevice() {
+        const size_t n = (size_t)(nnz > 0 ? nnz : 1);
+        cudaMalloc(&d_rowIdx, sizeof(int) * n);
+        cudaMalloc(&d_colIdx, sizeof(int) * n);
+        cudaMalloc(&d_values, sizeof(FloatType) * n);
+        ownsDeviceMemory = true;
+    }
+    void copyToDevice(cudaStream_t stream = 0) {
+        if (nnz <= 0) return;
+        cudaMemcpyAsync(d_rowIdx, rowIdx, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, stream);
+        cudaMemcpyAsync(d_colIdx, colIdx, sizeof(int) * (size_t)nnz, cudaMemcpyHostToDevice, stream);
+        cudaMemcpyAsync(d_values, values, sizeof(FloatType) * (size_t)nnz, cudaMemcpyHostToDevice, stream);
+    }
+};
+
+// CSR2Matrix<T> (sparse_formats.h:164-205) and BSRMatrix<T, B>
+// (sparse_formats.h:207-269): declared by the reference without kernels or
+// conversions; the same members here, so code naming them compiles.
+// spmv_exec refuses both formats (SPMV_ERROR_UNSUPPORTED_FORMAT).
+template <typename FloatType>
+struct CSR2Matrix {
+    int numRows = 0, numCols = 0, nnz = 0;
+    int* rowPtr = nullptr;
+    FloatType* values = nullptr;
+    uint8_t* metadata = nullptr;
+    int* d_rowPtr = nullptr;
+    FloatType* d_values = nullptr;
+    uint8_t* d_metadata = nullptr;
+    bool ownsHostMemory = false;
+    bool ownsDeviceMemory = false;
+};
+
+template <typename FloatType, int BlockSize>
+struct BSRMatrix {
+    int numRows = 0, numCols = 0, numBlockRows = 0, numBlockCols = 0, numBlocks = 0;
+    int blockSize = BlockSize;
+    int* rowPtr = nullptr;
+    int* colIdx = nullptr;
+    FloatType* values = nullptr;
+    int* d_rowPtr = nullptr;
+    int* d_colIdx = nullptr;
+    FloatType* d_values = nullptr;
+    bool ownsHostMemory = false;
+    bool ownsDeviceMemory = false;
+};
+
 template <typename FloatType>
 struct ELLPACKMatrix {
     int numRows = 0, numCols = 0, numElements = 0, nnz = 0;
@@ -303,8 +389,9 @@ spmv_status_t spmv_ellpack(const ELLPACKMatrix<FloatType>& ellpack, const FloatT
 }
 
 // spmv_exec<T> (spmv_api.h:57-65, declared but not defined by the reference):
-// `matrix` points to a CSRMatrix<T>, CSR5Matrix<T> or ELLPACKMatrix<T>
-// according to `format`; runs on the handle's stream and options.
+// `matrix` points to a CSRMatrix<T>, CSR5Matrix<T>, COOMatrix<T> or
+// ELLPACKMatrix<T> according to `format`; runs on the handle's stream and
+// options.  CSR2 and BSR are refused.
 template <typename FloatType>
 spmv_status_t spmv_exec(spmv_handle_t* handle, spmv_format_t format, const void* matrix, const FloatType* x,
                         FloatType* y, FloatType alpha = 1.0, FloatType beta = 0.0) {
@@ -317,6 +404,16 @@ spmv_status_t spmv_exec(spmv_handle_t* handle, spmv_format_t format, const void*
             return spmv_csr<FloatType>(*static_cast<const CSRMatrix<FloatType>*>(matrix), x, y, alpha, beta, o);
         case SPMV_FORMAT_CSR5:
             return spmv_csr5<FloatType>(*static_cast<const CSR5Matrix<FloatType>*>(matrix), x, y, alpha, beta, o);
+        case SPMV_FORMAT_COO: {
+            const auto& c = *static_cast<const COOMatrix<FloatType>*>(matrix);
+            if (std::is_same<FloatType, float>::value)
+                return spmv_coo_f32(c.numRows, c.numCols, c.nnz, c.d_rowIdx, c.d_colIdx,
+                                    reinterpret_cast<const float*>(c.d_values), reinterpret_cast<const float*>(x),
+                                    reinterpret_cast<float*>(y), (float)alpha, (float)beta, &o);
+            return spmv_coo_f64(c.numRows, c.numCols, c.nnz, c.d_rowIdx, c.d_colIdx,
+                                reinterpret_cast<const double*>(c.d_values), reinterpret_cast<const double*>(x),
+                                reinterpret_cast<double*>(y), (double)alpha, (double)beta, &o);
+        }
         case SPMV_FORMAT_ELL: {
             const auto& e = *static_cast<const ELLPACKMatrix<FloatType>*>(matrix);
             if (std::is_same<FloatType, float>::value)

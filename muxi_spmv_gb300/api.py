@@ -154,6 +154,51 @@ def spmv_csr(A: CSRMatrix, x, y, alpha=1.0, beta=0.0, opts: Opts | None = None):
     return y
 
 
+class COOMatrix:
+    """COOMatrix<T> (src/formats/sparse_formats.h:113-162): host arrays rowIdx,
+    colIdx, values (numpy) and device copies d_* (torch)."""
+
+    def __init__(self, rowIdx, colIdx, values, numRows: int, numCols: int):
+        self.rowIdx = np.ascontiguousarray(rowIdx, np.int32)
+        self.colIdx = np.ascontiguousarray(colIdx, np.int32)
+        self.values = np.ascontiguousarray(values)
+        self.numRows, self.numCols, self.nnz = int(numRows), int(numCols), len(self.values)
+        self.d_rowIdx = self.d_colIdx = self.d_values = None
+
+    def copyToDevice(self, device="cuda"):
+        torch = _torch()
+        self.d_rowIdx = torch.from_numpy(self.rowIdx.copy() if self.nnz else np.zeros(1, np.int32)).to(device)
+        self.d_colIdx = torch.from_numpy(self.colIdx.copy() if self.nnz else np.zeros(1, np.int32)).to(device)
+        self.d_values = torch.from_numpy(self.values.copy() if self.nnz else np.zeros(1, self.values.dtype)).to(device)
+        return self
+
+    def device_args(self):
+        return (self.numRows, self.numCols, self.nnz, _ptr(self.d_rowIdx), _ptr(self.d_colIdx), _ptr(self.d_values))
+
+
+def coo_to_csr(A: COOMatrix, stream=None) -> CSRMatrix:
+    """Device CSR of a COO matrix (entries ordered by row, then column)."""
+    torch = _torch()
+    dev = A.d_values.device
+    rp = torch.empty(A.numRows + 1, dtype=torch.int32, device=dev)
+    ci = torch.empty(max(A.nnz, 1), dtype=torch.int32, device=dev)
+    va = torch.empty(max(A.nnz, 1), dtype=A.d_values.dtype, device=dev)
+    f = lib().spmv_coo_to_csr_f32 if A.values.dtype == np.float32 else lib().spmv_coo_to_csr_f64
+    check(f(*A.device_args(), _ptr(rp), _ptr(ci), _ptr(va), _stream_ptr(stream)), "spmv_coo_to_csr")
+    B = CSRMatrix(np.zeros(A.numRows + 1, np.int32), np.zeros(0, np.int32), np.zeros(0, A.values.dtype), A.numCols)
+    B.nnz = A.nnz
+    B.d_rowPtr, B.d_colIdx, B.d_values = rp, ci, va
+    return B
+
+
+def spmv_coo(A: COOMatrix, x, y, alpha=1.0, beta=0.0, opts: Opts | None = None):
+    """y = alpha*A*x + beta*y for a COO matrix (converted per call)."""
+    o = opts if opts is not None else spmv_default_opts()
+    f = lib().spmv_coo_f32 if A.values.dtype == np.float32 else lib().spmv_coo_f64
+    check(f(*A.device_args(), _ptr(x), _ptr(y), alpha, beta, C.byref(o)), "spmv_coo")
+    return y
+
+
 def spmv_csr_transpose(A: CSRMatrix, x, y, alpha=1.0, beta=0.0, stream=None):
     """y = alpha*A^T*x + beta*y (the reference's spmv_exec_transpose, spmv_api.h:70-78)."""
     o = spmv_default_opts(stream)

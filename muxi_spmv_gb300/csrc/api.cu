@@ -251,6 +251,36 @@ static spmv_status_t csr_exec(const spmv_variant_t* v, int R, int C, int N, cons
     return finish<T>(opts, s);
 }
 
+// COO SpMV: the matrix is converted to CSR in stream-ordered scratch
+// (coo_to_csr), then runs as the stateless CSR call.
+template <typename T>
+static spmv_status_t coo_exec(int R, int C, int N, const int* rowIdx, const int* colIdx, const T* values, const T* x,
+                              T* y, T alpha, T beta, const spmv_opts_t* opts) {
+    clear_error();
+    if (R < 0 || C < 0 || N < 0) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "negative dimension");
+    if (opts && opts->operation != SPMV_OP_NORMAL)
+        MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "COO SpMV supports SPMV_OP_NORMAL only");
+    const cudaStream_t s = opts_stream(opts);
+    const size_t ar = (sizeof(int) * ((size_t)R + 1) + 255) & ~size_t(255);
+    const size_t ac = (sizeof(int) * (size_t)N + 255) & ~size_t(255);
+    void* buf = nullptr;
+    MXS_TRY(scratch_alloc(&buf, ar + ac + sizeof(T) * (size_t)N + 16, s));
+    int* rp = static_cast<int*>(buf);
+    int* ci = reinterpret_cast<int*>(static_cast<char*>(buf) + ar);
+    T* va = reinterpret_cast<T*>(static_cast<char*>(buf) + ar + ac);
+    spmv_status_t st = coo_to_csr<T>(R, C, N, rowIdx, colIdx, values, rp, ci, va, s);
+    if (st == SPMV_SUCCESS) {
+        spmv_opts_t o = opts ? *opts : spmv_default_opts();
+        o.sync = 0;
+        st = csr_exec<T>(nullptr, R, C, N, rp, ci, va, x, y, alpha, beta, &o);
+    }
+    const spmv_status_t st2 = scratch_free(buf, s);
+    MXS_TRY(st);
+    MXS_TRY(st2);
+    if (opts && opts->sync) MXS_CUDA(cudaStreamSynchronize(s));
+    return SPMV_SUCCESS;
+}
+
 }  // namespace mxs
 
 using namespace mxs;
@@ -366,6 +396,15 @@ spmv_status_t spmv_merge_path_search(const int* rowPtr, int numRows, int nnz, co
     clear_error();
     if (numRows < 0 || nnz < 0) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "negative dimension");
     return merge_search(rowPtr, numRows, nnz, diag, count, rowIdx, nnzIdx, stream);
+}
+
+spmv_status_t spmv_coo_f32(int R, int C, int N, const int* rowIdx, const int* colIdx, const float* values,
+                           const float* x, float* y, float alpha, float beta, const spmv_opts_t* opts) {
+    return coo_exec<float>(R, C, N, rowIdx, colIdx, values, x, y, alpha, beta, opts);
+}
+spmv_status_t spmv_coo_f64(int R, int C, int N, const int* rowIdx, const int* colIdx, const double* values,
+                           const double* x, double* y, double alpha, double beta, const spmv_opts_t* opts) {
+    return coo_exec<double>(R, C, N, rowIdx, colIdx, values, x, y, alpha, beta, opts);
 }
 
 spmv_status_t spmv_merge_based_f32(int R, int C, int N, const int* rowPtr, const int* colIdx, const float* values,

@@ -177,4 +177,15 @@ spmv_status_t spmv_csr_transpose_f64(int R, int C, int N, const int* rowPtr, con
     return csr_transpose<double>(R, C, N, rowPtr, colIdx, values, tRowPtr, tColIdx, tValues, stream);
 }
 
+spmv_status_t spmv_coo_to_csr_f32(int R, int C, int N, const int* rowIdx, const int* colIdx, const float* values,
+                                  int* rowPtr, int* outColIdx, float* outValues, cudaStream_t stream) {
+    clear_error();
+    return coo_to_csr<float>(R, C, N, rowIdx, colIdx, values, rowPtr, outColIdx, outValues, stream);
+}
+spmv_status_t spmv_coo_to_csr_f64(int R, int C, int N, const int* rowIdx, const int* colIdx, const double* values,
+                                  int* rowPtr, int* outColIdx, double* outValues, cudaStream_t stream) {
+    clear_error();
+    return coo_to_csr<double>(R, C, N, rowIdx, colIdx, values, rowPtr, outColIdx, outValues, stream);
+}
+
 }  // extern "C"

@@ -35,5 +35,11 @@ spmv_status_t sort_within_rows(int numRows, int numCols, int nnz, const int* row
 template <typename T>
 spmv_status_t csr_transpose(int numRows, int numCols, int nnz, const int* rowPtr, const int* colIdx, const T* values,
                             int* tRowPtr, int* tColIdx, T* tValues, cudaStream_t s);
+// CSR of a COO matrix: entries ordered by (row, column), equal pairs in input
+// order (they stay separate entries, which add); entries outside the matrix
+// are refused (synchronises the stream to check).
+template <typename T>
+spmv_status_t coo_to_csr(int numRows, int numCols, int nnz, const int* rowIdx, const int* colIdx, const T* values,
+                         int* rowPtr, int* outCol, T* outVal, cudaStream_t s);
 
 }  // namespace mxs

@@ -578,4 +578,99 @@ template spmv_status_t csr_transpose<float>(int, int, int, const int*, const int
 template spmv_status_t csr_transpose<double>(int, int, int, const int*, const int*, const double*, int*, int*,
                                              double*, cudaStream_t);
 
+// ---------------------------------------------------------------------------
+// COO -> CSR: entries ordered by (row, column) with two stable radix sorts
+// (column, then row; equal (row, column) pairs keep their input order), row
+// counts scanned into rowPtr, and a gather of columns and values.
+// ---------------------------------------------------------------------------
+__global__ void count_keys_kernel(long long n, const int* __restrict__ key, unsigned* __restrict__ cnt) {
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        atomicAdd(cnt + key[k], 1u);
+}
+__global__ void gather_keys_kernel(long long n, const unsigned* __restrict__ pos, const int* __restrict__ src,
+                                   unsigned* __restrict__ dst) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[k] = (unsigned)src[pos[k]];
+}
+__global__ void coo_bad_kernel(long long n, const int* __restrict__ row, const int* __restrict__ col, int R, int C,
+                               unsigned* __restrict__ bad) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n && ((unsigned)row[k] >= (unsigned)R || (unsigned)col[k] >= (unsigned)C)) atomicAdd(bad, 1u);
+}
+template <typename T>
+__global__ void coo_gather_kernel(long long n, const unsigned* __restrict__ pos, const int* __restrict__ col,
+                                  const T* __restrict__ val, int* __restrict__ outCol, T* __restrict__ outVal) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const unsigned p = pos[k];
+    outCol[k] = col[p];
+    outVal[k] = val[p];
+}
+
+template <typename T>
+spmv_status_t coo_to_csr(int numRows, int numCols, int nnz, const int* rowIdx, const int* colIdx, const T* values,
+                         int* rowPtr, int* outCol, T* outVal, cudaStream_t s) {
+    if (numRows < 0 || numCols < 0 || nnz < 0) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "negative dimension");
+    if (!rowPtr) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "rowPtr is NULL");
+    if (nnz == 0) {
+        MXS_CUDA(cudaMemsetAsync(rowPtr, 0, sizeof(int) * ((size_t)numRows + 1), s));
+        return SPMV_SUCCESS;
+    }
+    if (!rowIdx || !colIdx || !values || !outCol || !outVal) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "NULL array");
+    const size_t n = (size_t)nnz;
+    const size_t a = (sizeof(unsigned) * n + 255) & ~size_t(255);
+    const size_t ar = (sizeof(unsigned) * ((size_t)numRows + 1) + 255) & ~size_t(255);
+    void* buf = nullptr;
+    MXS_TRY(scratch_alloc(&buf, 2 * a + ar + 256, s));
+    char* b = static_cast<char*>(buf);
+    unsigned* keys = reinterpret_cast<unsigned*>(b);
+    unsigned* pos = reinterpret_cast<unsigned*>(b + a);
+    unsigned* cnt = reinterpret_cast<unsigned*>(b + 2 * a);
+    unsigned* bad = reinterpret_cast<unsigned*>(b + 2 * a + ar);
+    const unsigned g = grid_for(nnz, 256);
+    unsigned hbad = 0;
+    cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(unsigned), s);
+    if (e == cudaSuccess) {
+        coo_bad_kernel<<<g, 256, 0, s>>>(nnz, rowIdx, colIdx, numRows, numCols, bad);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hbad, bad, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    spmv_status_t st = e == cudaSuccess ? SPMV_SUCCESS : cuda_fail(e, "COO to CSR", __FILE__, __LINE__);
+    if (st == SPMV_SUCCESS && hbad) {
+        set_error(__FILE__, __LINE__, "%u COO entries lie outside the %d x %d matrix", hbad, numRows, numCols);
+        st = SPMV_ERROR_INVALID_MATRIX;
+    }
+    if (st == SPMV_SUCCESS) {
+        e = cudaMemcpyAsync(keys, colIdx, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(unsigned) * ((size_t)numRows + 1), s);
+        if (e == cudaSuccess) {
+            iota_kernel<<<g, 256, 0, s>>>(pos, nnz);
+            count_keys_kernel<<<g < 4096u ? g : 4096u, 256, 0, s>>>(nnz, rowIdx, cnt);
+            e = cudaGetLastError();
+        }
+        if (e != cudaSuccess) st = cuda_fail(e, "COO to CSR", __FILE__, __LINE__);
+    }
+    if (st == SPMV_SUCCESS) st = radix_sort_pairs(keys, pos, nnz, bits_for(numCols > 0 ? numCols - 1 : 0), s);
+    if (st == SPMV_SUCCESS) {
+        gather_keys_kernel<<<g, 256, 0, s>>>(nnz, pos, rowIdx, keys);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) st = cuda_fail(e, "COO to CSR", __FILE__, __LINE__);
+    }
+    if (st == SPMV_SUCCESS) st = radix_sort_pairs(keys, pos, nnz, bits_for(numRows > 0 ? numRows - 1 : 0), s);
+    if (st == SPMV_SUCCESS) st = scan_exclusive_u32(cnt, reinterpret_cast<unsigned*>(rowPtr), numRows + 1, nullptr, s);
+    if (st == SPMV_SUCCESS) {
+        coo_gather_kernel<T><<<g, 256, 0, s>>>(nnz, pos, colIdx, values, outCol, outVal);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) st = cuda_fail(e, "COO to CSR", __FILE__, __LINE__);
+    }
+    scratch_free(buf, s);
+    return st;
+}
+template spmv_status_t coo_to_csr<float>(int, int, int, const int*, const int*, const float*, int*, int*, float*,
+                                         cudaStream_t);
+template spmv_status_t coo_to_csr<double>(int, int, int, const int*, const int*, const double*, int*, int*, double*,
+                                          cudaStream_t);
+
 }  // namespace mxs
+

@@ -149,8 +149,28 @@ int main() {
     cudaStreamSynchronize(st);
     cudaMemcpy(y.data(), dy, m * sizeof(float), cudaMemcpyDeviceToHost);
     report("spmv_exec CSR5", status == SPMV_SUCCESS && close(y, want, scale));
-    report("spmv_exec COO unsupported", spmv_exec<float>(handle, SPMV_FORMAT_COO, &A, dx, dy) ==
-                                            SPMV_ERROR_UNSUPPORTED_FORMAT);
+    // COO (sparse_formats.h:113-162), entries in reverse order: converted on the device.
+    {
+        COOMatrix<float> coo;
+        coo.allocateHost(m, m, A.nnz);
+        int k = 0;
+        for (int r = m - 1; r >= 0; --r)
+            for (int j = A.rowPtr[r + 1] - 1; j >= A.rowPtr[r]; --j, ++k) {
+                coo.rowIdx[k] = r;
+                coo.colIdx[k] = A.colIdx[j];
+                coo.values[k] = A.values[j];
+            }
+        coo.allocateDevice();
+        coo.copyToDevice(st);
+        cudaMemset(dy, 0, m * sizeof(float));
+        status = spmv_exec<float>(handle, SPMV_FORMAT_COO, &coo, dx, dy);
+        cudaStreamSynchronize(st);
+        cudaMemcpy(y.data(), dy, m * sizeof(float), cudaMemcpyDeviceToHost);
+        report("spmv_exec COO", status == SPMV_SUCCESS && close(y, want, scale));
+    }
+    report("spmv_exec CSR2 / BSR unsupported",
+           spmv_exec<float>(handle, SPMV_FORMAT_CSR2, &A, dx, dy) == SPMV_ERROR_UNSUPPORTED_FORMAT &&
+               spmv_exec<float>(handle, SPMV_FORMAT_BSR, &A, dx, dy) == SPMV_ERROR_UNSUPPORTED_FORMAT);
 
     // spmv_exec_transpose (spmv_api.h:70-78): y = A^T x.
     {
