@@ -228,7 +228,9 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
 #pragma unroll
     for (int e = 0; e < E; ++e) g[e] = ld_x(x + L.c[e]);  // past nnz: c = 0, v = 0, unused
 
-    if (rFirst == rLast && t + 1 < tiles) {  // interior tile of one row
+    // Interior tile of one row.  Tile 0 takes it only when no empty rows
+    // precede its row: the row logic writes those leading rows.
+    if (rFirst == rLast && t + 1 < tiles && (t > 0 || rFirst == 0)) {
         T sum = T(0);
 #pragma unroll
         for (int e = 0; e < E; ++e) sum += L.v[e] * g[e];

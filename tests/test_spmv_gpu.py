@@ -39,6 +39,12 @@ def build_cases(mx):
     ci = rng.integers(0, 500, rp[-1]).astype(np.int32)
     v = rng.standard_normal(rp[-1]).astype(np.float32)
     cases["empties"] = (rp, ci, v, 500)
+    # Leading empty rows before a row longer than two tiles of every size: the
+    # first tile lies inside one row and must still write the empty rows.
+    lens = np.r_[np.zeros(7), 3000, rng.integers(0, 5, 40), np.zeros(5)].astype(np.int32)
+    rp = np.r_[0, np.cumsum(lens)].astype(np.int32)
+    ci = np.sort(rng.integers(0, 4000, rp[-1]).astype(np.int32))
+    cases["lead_empty_longrow"] = (rp, ci, rng.standard_normal(rp[-1]).astype(np.float32), 4000)
     cases["one_row"] = (np.array([0, 5], np.int32), np.array([0, 1, 1, 7, 9], np.int32),
                         np.array([1, 2, 3, 4, 5], np.float32), 10)
     cases["no_nnz"] = (np.zeros(33, np.int32), np.zeros(0, np.int32), np.zeros(0, np.float32), 33)
