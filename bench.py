@@ -120,6 +120,23 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(values, ws, device):
+    """Max of each value over the ranks (replicas: the job takes as long as
+    its slowest rank).  One all_reduce on `device` (NCCL on GPUs, gloo on CPU)."""
+    if ws <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def replica_throughput(ws, units_per_rank, ms):
+    """Whole-job rate: every rank processed `units_per_rank` in at most `ms`."""
+    return ws * units_per_rank / (ms * 1e-3)
+
+
 def make_matrix(mx, W, name, dtype, seed=0, scale_rows=0):
     spec = W.scaled(name, scale_rows, seed) if scale_rows else W.spec(name, seed)
     t = time.time()
@@ -344,18 +361,16 @@ def gpu_arm(args):
         del Acsr
     clocks.stop()
 
+    step_ms, e2e_ms, serial_ms = max_over_ranks([step_ms, e2e_ms, serial_ms], ws, dev)
     if ws > 1:
-        t = torch.tensor([step_ms, e2e_ms, serial_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms, e2e_ms, serial_ms = t.tolist()
         dist.barrier()
 
     peak, peak_kind = peaks()
     kern_ms = kern_ms_total / max(kern_launches, 1)
     achieved = nbytes / (kern_ms * 1e-3) / 1e9
-    value = ws * nbytes / (step_ms * 1e-3) / 1e9
-    e2e_val = ws * nbytes / (e2e_ms * 1e-3) / 1e9
-    serial_val = ws * nbytes / (serial_ms * 1e-3) / 1e9
+    value = replica_throughput(ws, nbytes, step_ms) / 1e9
+    e2e_val = replica_throughput(ws, nbytes, e2e_ms) / 1e9
+    serial_val = replica_throughput(ws, nbytes, serial_ms) / 1e9
     pv = plan.variant.as_dict()
     kern_names = {mx.KERNEL_MERGE: "merge_vec_kernel",
                   mx.KERNEL_CSR5: "csr5_ordered_kernel" if pv["vectorWidth"] == 32 else "csr5_tile_kernel",
@@ -567,10 +582,7 @@ def batched_arm(args):
         torch.cuda.synchronize(dev)
         e2e_ms = f0.elapsed_time(f1) / args.steps
         clocks.stop()
-        if ws > 1:
-            t = torch.tensor([times["persistent_graph"], e2e_ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            times["persistent_graph"], e2e_ms = t.tolist()
+        times["persistent_graph"], e2e_ms = max_over_ranks([times["persistent_graph"], e2e_ms], ws, dev)
 
         ms = times["persistent_graph"]
         achieved = nbytes / (ms * 1e-3) / 1e9
