@@ -560,7 +560,25 @@ def batched_arm(args):
         times["plain_loop"] = e0.elapsed_time(e1) / plain_steps
         for p_ in plans:
             p_.destroy()
-        del plans, xcols, ycols
+        del plans
+
+        # the same loop through the reference's own entry point: spmv_csr<T>
+        # per matrix and right-hand side (stateless: tiles found every call)
+        opts = mx.spmv_default_opts(stream)
+
+        def stateless_once():
+            for A, xc, yc in zip(mats, xcols, ycols):
+                for j in range(k):
+                    mx.spmv_csr(A, xc[j], yc[j], 1.0, 0.0, opts)
+        stateless_once()
+        stream.synchronize()
+        e0.record(stream)
+        for _ in range(plain_steps):
+            stateless_once()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        times["spmv_csr_loop"] = e0.elapsed_time(e1) / plain_steps
+        del xcols, ycols
 
         # end to end: pinned host X in, Y out, persistent graph in between
         Xh = torch.empty(xn, dtype=torch.float32).pin_memory()
@@ -599,6 +617,9 @@ def batched_arm(args):
                            "variant": best_v,
                            "autotune_ms": {",".join(map(str, key)): round(t, 4) for key, t in tune_ms.items()},
                            "speedup_vs_plain_loop": round(times["plain_loop"] / ms, 3),
+                           "speedup_vs_spmv_csr_loop": round(times["spmv_csr_loop"] / ms, 3),
+                           "spmv_csr_loop": "per matrix and right-hand side: one spmv_csr_f32 call (the reference's "
+                                            "spmv_csr<T>, stateless: CSR5 tiles found per call, 3 launches)",
                            "plain_loop": "per matrix: one single-matrix plan (default AUTO variant), one "
                                          "spmv_plan_exec_f32 per right-hand side, 2 launches each",
                            "speedup_vs_loop": round(times["loop"] / ms, 3),
