@@ -382,8 +382,11 @@ def gpu_arm(args):
     traffic = None
     tf = ROOT / "profiles" / f"traffic_{args.workload}_{args.dtype}.json"
     if tf.exists() and perm is None and not args.scale_rows:
-        try:
-            traffic = json.loads(tf.read_text()).get("dram_bytes_per_launch")
+        try:  # a capture of this workload's dominant kernel, for the variant it was taken with
+            rec = json.loads(tf.read_text())
+            if list(rec.get("variant", [])) == [pv[k] for k in ("kernel", "blockSize", "threadsPerRow",
+                                                                 "itemsPerThread", "vectorWidth")]:
+                traffic = rec.get("dram_bytes_per_launch")
         except Exception:
             traffic = None
 
