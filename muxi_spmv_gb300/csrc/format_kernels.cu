@@ -537,7 +537,9 @@ static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* ca
         a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha, a.beta, a.betaZero, tileRow, tiles,   \
         carryRow, carryVal, a.noEmptyRows, bits)
         switch (block) {
-            case 128: MXS_ORDERED(128, wide ? 6 : 16); break;
+            // 16 four-byte or 8 eight-byte values per lane: 10 blocks (48
+            // registers, 40 warps) measured best; 16 doubles need 6.
+            case 128: MXS_ORDERED(128, E * sizeof(T) >= 128 ? 6 : (wide ? 10 : 16)); break;
             case 256: MXS_ORDERED(256, wide ? 3 : 6); break;
             case 512: MXS_ORDERED(512, wide ? 2 : 4); break;
             case 1024: MXS_ORDERED(1024, wide ? 1 : 2); break;

@@ -10,6 +10,15 @@
 
 namespace mxs {
 
+spmv_variant_t auto_variant(spmv_type_t type, int nnz) {
+    // Without a selector model: CSR5 tiles with gathers in nonzero order,
+    // 128-thread blocks (nnz-balanced, warp-local, the fastest measured
+    // variant on irregular matrices) -- 512-nonzero tiles for FP32, 256 for
+    // FP64; merge-path tiles when the nonzero count is beyond CSR5's range.
+    if (nnz > 0x7fffffff - 32768) return spmv_variant_t{SPMV_KERNEL_MERGE, 256, 0, 8, 4};
+    return spmv_variant_t{SPMV_KERNEL_CSR5, 128, 0, type == SPMV_TYPE_DOUBLE ? 8 : 16, 32};
+}
+
 spmv_variant_t heuristic_variant(int numRows, int nnz) {
     const int avg = nnz / (numRows > 1 ? numRows : 1);
     spmv_variant_t v{};
@@ -25,18 +34,11 @@ spmv_variant_t heuristic_variant(int numRows, int nnz) {
     return v;
 }
 
-static spmv_variant_t resolve(const spmv_variant_t* req, int R, int N) {
+static spmv_variant_t resolve(const spmv_variant_t* req, spmv_type_t type, int R, int N) {
     spmv_variant_t v{};
     if (req) v = *req;
     if (v.kernel == SPMV_KERNEL_HEURISTIC) return heuristic_variant(R, N);
-    if (v.kernel == SPMV_KERNEL_AUTO) {
-        // Without a selector model: CSR5 tiles of 256 nonzeros with gathers in
-        // nonzero order, 128-thread blocks (nnz-balanced, warp-local, the
-        // fastest measured variant on irregular matrices); merge-path tiles
-        // when the nonzero count is beyond CSR5's range.
-        if (N > 0x7fffffff - 32768) return spmv_variant_t{SPMV_KERNEL_MERGE, 256, 0, 8, 4};
-        return spmv_variant_t{SPMV_KERNEL_CSR5, 128, 0, 8, 32};
-    }
+    if (v.kernel == SPMV_KERNEL_AUTO) return auto_variant(type, N);
     if (!v.blockSize) v.blockSize = 256;
     if (v.kernel == SPMV_KERNEL_SCALAR) v.threadsPerRow = 1;
     if (v.kernel == SPMV_KERNEL_VECTOR && !v.threadsPerRow) v.threadsPerRow = 32;
@@ -117,14 +119,14 @@ static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T
 
 spmv_status_t plan_variant(spmv_handle_t* h, spmv_type_t type, int R, int C, int N, const int* rowPtr,
                            const int* colIdx, const spmv_variant_t* variant, spmv_variant_t* out) {
-    *out = resolve(variant, R, N);
+    *out = resolve(variant, type, R, N);
     const HandleState* hs = static_cast<const HandleState*>(h->internal);
     if ((!variant || variant->kernel == SPMV_KERNEL_AUTO) && hs && hs->selector && R > 0 && N > 0) {
         std::vector<int> order;
         MXS_TRY(learned_rank(hs->selector, type, R, C, N, rowPtr, colIdx, h->stream, order));
         std::vector<spmv_variant_t> space(spmv_variant_space(nullptr, 0));
         spmv_variant_space(space.data(), (int)space.size());
-        *out = resolve(&space[order[0]], R, N);
+        *out = resolve(&space[order[0]], type, R, N);
     }
     return SPMV_SUCCESS;
 }

@@ -48,6 +48,8 @@ namespace mxs {
 // The reference's NVIDIA dispatch rule (spmv_csr.cu:115-153): integer
 // avgNnz = nnz / rows; scalar kernel below 32, one warp per row from 32 up.
 spmv_variant_t heuristic_variant(int numRows, int nnz);
+// The AUTO plan's variant without a selector model (plan.cu).
+spmv_variant_t auto_variant(spmv_type_t type, int nnz);
 // Learned selector: indices into the variant space of the variants that
 // apply to this matrix, best predicted first (select.cu).
 spmv_status_t learned_rank(spmv_mlp_t model, spmv_type_t type, int R, int C, int N, const int* rowPtr,

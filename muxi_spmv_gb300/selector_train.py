@@ -43,7 +43,7 @@ LAWS = ("poisson", "zipf", "banded", "blockdiag", "stencil")
 # it the law is LAWS[seed % 4].
 STENCIL_SEED0 = 1_000_000
 HEURISTIC_COL = -1  # last column of the label matrix: the heuristic's variant
-DEFAULT_VARIANT = Variant(api.KERNEL_CSR5, 128, 0, 8, 32)  # the AUTO plan without a model
+DEFAULT_VARIANT = Variant(api.KERNEL_CSR5, 128, 0, 16, 32)  # the FP32 AUTO plan without a model
 
 
 def _zipf_clip_for_mean(s: float, target: float, cap: int) -> int:
