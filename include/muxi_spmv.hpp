@@ -301,6 +301,18 @@ spmv_status_t spmv_merge_based(const CSRMatrix<FloatType>& matrix, const FloatTy
     return merge_call(matrix, x, y, stream);
 }
 
+// spmv_sparse_optimized<T> (src/spmv/csr/spmv_sparse_optimized.cuh:29-33):
+// the reference picks a light / virtual-warp / merge kernel by mean row
+// length; here every matrix takes the stateless default (per-call CSR5 tiles,
+// nonzero-balanced, so short and long rows alike), y = A*x on `stream`.
+template <typename FloatType>
+spmv_status_t spmv_sparse_optimized(const CSRMatrix<FloatType>& matrix, const FloatType* x, FloatType* y,
+                                    cudaStream_t stream) {
+    spmv_opts_t o = spmv_default_opts();
+    o.stream = reinterpret_cast<void*>(stream);
+    return spmv_csr<FloatType>(matrix, x, y, FloatType(1), FloatType(0), o);
+}
+
 template <typename FloatType>
 spmv_status_t csr5_preprocess(const CSRMatrix<FloatType>& csr, CSR5Matrix<FloatType>& csr5, int sigma,
                               cudaStream_t stream) {

@@ -1,6 +1,7 @@
 // Drop-in check: reference-style call sites (tests/correctness/test_spmv.cu,
 // tests/benchmark/test_runner.cu:265-329, src/benchmark/performance_benchmark.cu:
-// 383-422, tests/benchmark/test_ellpack.cu:46-115) compiled unchanged against
+// 383-422, tests/benchmark/test_ellpack.cu:46-115, tests/test_sparse_optimized.cu:80)
+// compiled unchanged against
 // include/muxi_spmv.hpp and linked to libmuxispmv.so.  Prints PASSED/FAILED
 // per check and exits non-zero on any failure.
 #include <cmath>
@@ -112,6 +113,10 @@ int main() {
     status = spmv_merge_based<float>(A, dx, dy, 0);
     fetch();
     report("spmv_merge_based", status == SPMV_SUCCESS && close(y, want, scale));
+
+    status = spmv_sparse_optimized<float>(A, dx, dy, 0);  // tests/test_sparse_optimized.cu:80
+    fetch();
+    report("spmv_sparse_optimized", status == SPMV_SUCCESS && close(y, want, scale));
 
     CSR5Matrix<float> csr5;
     status = csr5_preprocess<float>(A, csr5, 0, 0);
