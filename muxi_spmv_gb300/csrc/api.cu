@@ -142,13 +142,13 @@ spmv_status_t merge_stateless(const MergeGeom& g, const RowsArgs<T>& a, cudaStre
     return st != SPMV_SUCCESS ? st : st2;
 }
 
-// The default stateless SpMV: CSR5 tiles found for this call (one binary
-// search per tile; 512 nonzeros for FP32, 256 for FP64, as in AUTO plans),
-// the ordered tile kernel (128-thread blocks) and the tile-walking carry
-// fix-up, all in stream-ordered scratch.
+// The default stateless SpMV: CSR5 tiles of 256 nonzeros found for this call
+// (one binary search per tile), the ordered tile kernel (128-thread blocks)
+// and the tile-walking carry fix-up, all in stream-ordered scratch.  (A call
+// has no row-start masks, without which 256-nonzero tiles beat 512.)
 template <typename T>
 spmv_status_t csr5_stateless(const RowsArgs<T>& a, cudaStream_t s) {
-    constexpr int kSigma = sizeof(T) == 4 ? 512 : 256;
+    constexpr int kSigma = 256;
     const long long tiles = ((long long)a.nnz + kSigma - 1) / kSigma;
     const size_t a4 = ((sizeof(int) * tiles) + 255) & ~size_t(255);
     void* buf = nullptr;

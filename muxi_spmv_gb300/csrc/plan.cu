@@ -13,8 +13,9 @@ namespace mxs {
 spmv_variant_t auto_variant(spmv_type_t type, int nnz) {
     // Without a selector model: CSR5 tiles with gathers in nonzero order,
     // 128-thread blocks (nnz-balanced, warp-local, the fastest measured
-    // variant on irregular matrices) -- 512-nonzero tiles for FP32, 256 for
-    // FP64; merge-path tiles when the nonzero count is beyond CSR5's range.
+    // variant on irregular matrices) -- 512-nonzero tiles for FP32 (256 when
+    // the matrix has empty rows, plan_variant), 256 for FP64; merge-path
+    // tiles when the nonzero count is beyond CSR5's range.
     if (nnz > 0x7fffffff - 32768) return spmv_variant_t{SPMV_KERNEL_MERGE, 256, 0, 8, 4};
     return spmv_variant_t{SPMV_KERNEL_CSR5, 128, 0, type == SPMV_TYPE_DOUBLE ? 8 : 16, 32};
 }
@@ -121,7 +122,16 @@ spmv_status_t plan_variant(spmv_handle_t* h, spmv_type_t type, int R, int C, int
                            const int* colIdx, const spmv_variant_t* variant, spmv_variant_t* out) {
     *out = resolve(variant, type, R, N);
     const HandleState* hs = static_cast<const HandleState*>(h->internal);
-    if ((!variant || variant->kernel == SPMV_KERNEL_AUTO) && hs && hs->selector && R > 0 && N > 0) {
+    const bool autoPick = !variant || variant->kernel == SPMV_KERNEL_AUTO;
+    if (autoPick && !(hs && hs->selector) && out->kernel == SPMV_KERNEL_CSR5 && out->itemsPerThread == 16 && R > 0) {
+        // 512-nonzero tiles pay with plan-time row-start masks, which need a
+        // matrix without empty rows; otherwise the tile's row search reads
+        // rowPtr slices that 512-nonzero tiles overflow: take 256.
+        long long empties = 0;
+        MXS_TRY(count_empty_rows(rowPtr, R, &empties, h->stream));
+        if (empties > 0) out->itemsPerThread = 8;
+    }
+    if (autoPick && hs && hs->selector && R > 0 && N > 0) {
         std::vector<int> order;
         MXS_TRY(learned_rank(hs->selector, type, R, C, N, rowPtr, colIdx, h->stream, order));
         std::vector<spmv_variant_t> space(spmv_variant_space(nullptr, 0));
