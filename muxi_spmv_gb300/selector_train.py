@@ -8,7 +8,8 @@ corpus: seeded matrices generated on the GPU, one law per seed -- Poisson row
 lengths, Zipf lengths (s in [1.3, 2.5]), banded (width 3..1025) and
 block-diagonal (8..256 blocks) -- with rows log-uniform in [1e4, 1e7] and mean
 row length log-uniform in [2, 128], FP32 N(0,1) values; seeds from
-STENCIL_SEED0 on are grid stencils (2D 5-point, 3D 27-point).  Each matrix gets its
+STENCIL_SEED0 on are grid stencils (2D 5-point, 3D 27-point), from
+POWERLAW_SEED0 on power-law rows with a near-diagonal share.  Each matrix gets its
 32 features (spmv_matrix_features) and the exhaustive autotuner's time for
 every variant of the space plus the reference heuristic's pick.  Records are
 written in chunks, so an interrupted run resumes where it stopped.
@@ -35,13 +36,16 @@ from pathlib import Path
 import numpy as np
 
 from . import api, selector
-from .api import (GenSpec, GEN_BANDED, GEN_BLOCKDIAG, GEN_POISSON_UNIFORM, GEN_STENCIL2D, GEN_STENCIL3D,
-                  GEN_ZIPF_UNIFORM, Variant)
+from .api import (GenSpec, GEN_BANDED, GEN_BLOCKDIAG, GEN_POISSON_UNIFORM, GEN_POWERLAW, GEN_STENCIL2D,
+                  GEN_STENCIL3D, GEN_ZIPF_UNIFORM, Variant)
 
-LAWS = ("poisson", "zipf", "banded", "blockdiag", "stencil")
-# Seeds from here on draw grid stencils (2D 5-point or 3D 27-point); below
-# it the law is LAWS[seed % 4].
+LAWS = ("poisson", "zipf", "banded", "blockdiag", "stencil", "powerlaw")
+# Seeds from STENCIL_SEED0 draw grid stencils (2D 5-point or 3D 27-point),
+# from POWERLAW_SEED0 power-law rows with a near-diagonal share (the
+# benchmark's law, generated on the host); below both the law is
+# LAWS[seed % 4].
 STENCIL_SEED0 = 1_000_000
+POWERLAW_SEED0 = 2_000_000
 HEURISTIC_COL = -1  # last column of the label matrix: the heuristic's variant
 DEFAULT_VARIANT = Variant(api.KERNEL_CSR5, 128, 0, 16, 32)  # the FP32 AUTO plan without a model
 
@@ -58,6 +62,8 @@ def _zipf_clip_for_mean(s: float, target: float, cap: int) -> int:
 def spec_for_seed(seed: int, max_rows: int = 10_000_000, max_nnz: int = 600_000_000):
     """The corpus matrix of `seed`: (GenSpec, law name, target mean row length)."""
     rng = np.random.default_rng(np.random.SeedSequence([0x5E1EC7, seed]))
+    if seed >= POWERLAW_SEED0:
+        return powerlaw_spec(rng, seed, max_rows)
     if seed >= STENCIL_SEED0:
         return stencil_spec(rng, seed, max_rows)
     law = LAWS[seed % 4] if seed >= 0 else LAWS[0]
@@ -103,6 +109,20 @@ def stencil_spec(rng, seed: int, max_rows: int):
     return spec, "stencil", 27.0
 
 
+def powerlaw_spec(rng, seed: int, max_rows: int):
+    """Zipf(s) row lengths, s in [1.5, 2.2], clipped at 256..65,536; a share
+    p in [0.3, 0.95] of the columns within +-band (band 64..8,192) of the
+    diagonal, the rest uniform; rows log-uniform 1e4..min(max_rows, 2e6)."""
+    gseed = 1_000_003 * seed + 17
+    R = int(round(10 ** rng.uniform(4, math.log10(min(max_rows, 2_000_000)))))
+    s = float(rng.uniform(1.5, 2.2))
+    clip = int(2 ** rng.integers(8, 17))
+    band = int(round(2 ** rng.uniform(6, 13)))
+    p = float(rng.uniform(0.3, 0.95))
+    spec = GenSpec(GEN_POWERLAW, R, R, s, float(min(clip, R)), float(min(band, R // 2)), p, gseed)
+    return spec, "powerlaw", 0.0
+
+
 def default_index() -> int:
     """Index in the variant space of the AUTO plan's variant without a model."""
     key = lambda v: (v.kernel, v.blockSize, v.threadsPerRow, v.itemsPerThread, v.vectorWidth)
@@ -121,7 +141,14 @@ def label_one(handle, seed: int, max_rows: int, max_nnz: int):
     """Generates, featurises and autotunes one corpus matrix."""
     import torch
     spec, law, m = spec_for_seed(seed, max_rows, max_nnz)
-    A = selector.gen_device(spec)
+    if law == "powerlaw":  # no device law: host generator, copied over
+        rp, ci, v = api.generate(spec)
+        A = selector.DeviceCSR(spec.numRows, spec.numCols, len(ci), torch.from_numpy(rp).cuda(),
+                               torch.from_numpy(ci if len(ci) else np.zeros(1, np.int32)).cuda(),
+                               torch.from_numpy(v if len(v) else np.zeros(1, np.float32)).cuda())
+        m = len(ci) / max(spec.numRows, 1)
+    else:
+        A = selector.gen_device(spec)
     torch.cuda.synchronize()
     feats = selector.matrix_features(A).cpu().numpy()
     space = selector.variant_space()
@@ -339,9 +366,9 @@ def main(argv=None):
     t.add_argument("--corpus", required=True)
     t.add_argument("--model", required=True)
     t.add_argument("--hidden", type=int, default=128)
-    t.add_argument("--epochs", type=int, default=400)
+    t.add_argument("--epochs", type=int, default=800)
     t.add_argument("--batch", type=int, default=128)
-    t.add_argument("--lr", type=float, default=2e-3)
+    t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--seed", type=int, default=0)
     t.add_argument("--report")
     t.add_argument("--merged", help="also write the combined records to this .npz")
