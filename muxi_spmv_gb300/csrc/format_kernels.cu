@@ -166,17 +166,22 @@ spmv_status_t csr5_tile_bits(const int* rowPtr, int numRows, int sigma, long lon
 
 // Products go through shared memory from nonzero order (lane l holds
 // nonzeros l + 32e) to lane-contiguous order (lane l takes l*E .. l*E+E-1).
-// For E >= 8 nonzero j sits at slot j + j/32: the writes (fixed e,
-// consecutive lanes) and the reads (fixed e, lanes E apart; the pad makes
-// E*l + l/(32/E) cover every bank once) are both free of bank conflicts for
-// 4-byte values.  For E = 4 the unpadded layout is already conflict-free (a
-// lane's four values are one 16-byte read, eight lanes per 128 bytes).
-template <int E>
+// For E >= 8 nonzero j sits at slot j + j/32 (4-byte values) or j + j/16
+// (8-byte values, served sixteen lanes at a time): the writes (fixed e,
+// consecutive lanes) and the reads (fixed e, lanes E apart; the pad spreads
+// them over every bank) are both free of bank conflicts.  For E = 4 the
+// unpadded layout is already conflict-free for 4-byte values (a lane's four
+// values are one 16-byte read, eight lanes per 128 bytes).
+template <typename T, int E>
 __device__ __forceinline__ int ordered_slot(int j) {
-    return E >= 8 ? j + (j >> 5) : j;
+    return E < 8 ? j : (sizeof(T) == 8 ? j + (j >> 4) : j + (j >> 5));
+}
+template <typename T, int E>
+constexpr int ordered_slots() {
+    return E < 8 ? 32 * E : (sizeof(T) == 8 ? 34 * E : 33 * E);
 }
 
-// sRp / sP: this warp's shared regions (kOrderedRpCap ints, 33E values).
+// sRp / sP: this warp's shared regions (kOrderedRpCap ints, ordered_slots values).
 // The rowPtr slice holds up to kOrderedRpCap entries (tiles spanning up to
 // 62 rows, nine in ten of the general tiles of a power-law matrix); a tile
 // over more rows reads rowPtr from global memory.  Small slices leave the
@@ -244,11 +249,11 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
 
     if (useBits) {
 #pragma unroll
-        for (int e = 0; e < E; ++e) sP[ordered_slot<E>(lane + 32 * e)] = L.v[e] * g[e];
+        for (int e = 0; e < E; ++e) sP[ordered_slot<T, E>(lane + 32 * e)] = L.v[e] * g[e];
         __syncwarp();
         T p[E];
 #pragma unroll
-        for (int e = 0; e < E; ++e) p[e] = sP[ordered_slot<E>(lane * E + e)];
+        for (int e = 0; e < E; ++e) p[e] = sP[ordered_slot<T, E>(lane * E + e)];
         csr5_tile_rows_bits<T, E>(p, L.bits, rFirst, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal);
         if (REUSE) __syncwarp();
         return;
@@ -263,11 +268,11 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
         }
     }
 #pragma unroll
-    for (int e = 0; e < E; ++e) sP[ordered_slot<E>(lane + 32 * e)] = L.v[e] * g[e];
+    for (int e = 0; e < E; ++e) sP[ordered_slot<T, E>(lane + 32 * e)] = L.v[e] * g[e];
     __syncwarp();
     T p[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) p[e] = sP[ordered_slot<E>(lane * E + e)];
+    for (int e = 0; e < E; ++e) p[e] = sP[ordered_slot<T, E>(lane * E + e)];
     csr5_tile_rows<T, E>(p, rFirst, rLast, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal,
                          [&](int r) { return (staged && r >= rFirst) ? sRp[r - rFirst] : __ldg(rowPtr + r); },
                          noEmpty);
@@ -300,7 +305,7 @@ csr5_ordered_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const 
                     T* __restrict__ carryVal, int noEmptyRows, const unsigned* __restrict__ tileBits) {
     constexpr int WARPS = BLOCK / 32;
     __shared__ int sRpAll[WARPS][kOrderedRpCap];
-    __shared__ __align__(16) T sPAll[WARPS][33 * E];
+    __shared__ __align__(16) T sPAll[WARPS][ordered_slots<T, E>()];
     pdl_trigger();  // the carry fix-up may be scheduled behind the last wave
     const long long t = ((long long)blockIdx.x * BLOCK + threadIdx.x) >> 5;
     if (t >= tiles) return;  // uniform per warp
@@ -325,7 +330,7 @@ csr5_ordered_range_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, 
                           const unsigned* __restrict__ tileBits) {
     constexpr int WARPS = BLOCK / 32;
     __shared__ int sRpAll[WARPS][kOrderedRpCap];
-    __shared__ __align__(16) T sPAll[WARPS][33 * E];
+    __shared__ __align__(16) T sPAll[WARPS][ordered_slots<T, E>()];
     __shared__ int sNext, sEnd;  // next tile to hand out, end of the range (shared: fewer live registers)
     pdl_trigger();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
