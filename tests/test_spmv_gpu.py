@@ -235,6 +235,41 @@ def test_plans(mx, cuda, handle, cases):
     p.destroy()
 
 
+def test_plan_exec_replays_from_a_cuda_graph(mx, cuda, cases):
+    """A plan allocates nothing at execution and its fix-up launch (with the
+    programmatic-dependent-launch attribute) captures: ten SpMVs recorded into
+    one CUDA graph replay with the same bits as direct executions."""
+    torch = cuda
+    for name in ("powerlaw60k", "empties", "lead_empty_longrow"):
+        rp, ci, v, cols = cases[name]
+        A = device_csr(mx, rp, ci, v, cols)
+        xh = mx.gen_vector(cols, 12)
+        x = torch.from_numpy(xh).cuda()
+        s = torch.cuda.Stream()
+        h = mx.spmv_create_handle()
+        h.set_stream(s)
+        for var in (None, mx.make_variant(mx.KERNEL_MERGE, 256, 0, 8, 4), mx.make_variant(mx.KERNEL_ELL)):
+            try:
+                p = mx.Plan(h, A, var)
+            except mx.SpmvError:
+                continue  # ELL refused (padding above 2x)
+            y_direct = torch.zeros(A.numRows, device="cuda")
+            with torch.cuda.stream(s):
+                p.exec(x, y_direct)
+            s.synchronize()
+            y = torch.zeros(A.numRows, device="cuda")
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=s):
+                for _ in range(10):
+                    p.exec(x, y)
+            y.zero_()
+            g.replay()
+            torch.cuda.synchronize()
+            assert torch.equal(y, y_direct), (name, var.as_dict() if var is not None else "auto")
+            p.destroy()
+        h.destroy()
+
+
 def test_stats(mx, cuda, cases):
     for name in ("powerlaw60k", "empties", "no_nnz"):
         rp, ci, v, cols = cases[name]
