@@ -611,7 +611,11 @@ typedef enum {
     SPMV_SELECT_HEURISTIC = 0,     /* the reference's mean-row-length rule      */
     SPMV_SELECT_LEARNED = 1,       /* features + MLP, argmin of predictions     */
     SPMV_SELECT_AUTOTUNE = 2,      /* time the whole space                      */
-    SPMV_SELECT_LEARNED_TOPK = 3   /* time only the model's topK best guesses   */
+    SPMV_SELECT_LEARNED_TOPK = 3,  /* time only the model's topK best guesses   */
+    SPMV_SELECT_LEARNED_FALLBACK = 4 /* learned pick; when other variants are
+                                        predicted within 2% of it (low
+                                        confidence), time those too (at most
+                                        topK, default 3) and take the fastest */
 } spmv_select_mode_t;
 
 /* Picks a variant for a device CSR matrix.  `model` is needed by the

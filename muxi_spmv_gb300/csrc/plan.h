@@ -53,7 +53,8 @@ spmv_variant_t auto_variant(spmv_type_t type, int nnz);
 // Learned selector: indices into the variant space of the variants that
 // apply to this matrix, best predicted first (select.cu).
 spmv_status_t learned_rank(spmv_mlp_t model, spmv_type_t type, int R, int C, int N, const int* rowPtr,
-                           const int* colIdx, cudaStream_t s, std::vector<int>& order);
+                           const int* colIdx, cudaStream_t s, std::vector<int>& order,
+                           std::vector<float>* predOut = nullptr);
 // The variant a plan on this matrix runs: AUTO / HEURISTIC resolved, the
 // learned pick when the handle has a selector model (plan.cu).
 spmv_status_t plan_variant(spmv_handle_t* h, spmv_type_t type, int R, int C, int N, const int* rowPtr,

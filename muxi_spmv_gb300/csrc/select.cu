@@ -42,14 +42,21 @@ static bool variant_applicable(const spmv_variant_t& v, int R, int N, long long 
     }
 }
 
+// Predicted log-time gap under which the learned pick counts as uncertain
+// (SPMV_SELECT_LEARNED_FALLBACK): 0.02, about 2%.
+constexpr float kFallbackMargin = 0.02f;
+
 static bool same_variant(const spmv_variant_t& a, const spmv_variant_t& b) {
     return a.kernel == b.kernel && a.blockSize == b.blockSize && a.threadsPerRow == b.threadsPerRow &&
            a.itemsPerThread == b.itemsPerThread && a.vectorWidth == b.vectorWidth;
 }
 
-// Space indices of the applicable variants, best predicted first.
+// Space indices of the applicable variants, best predicted first; `predOut`
+// (optional) receives the model's output per space index (predicted log of
+// the time over the best variant's).
 spmv_status_t learned_rank(spmv_mlp_t model, spmv_type_t type, int R, int C, int N, const int* rowPtr,
-                           const int* colIdx, cudaStream_t s, std::vector<int>& order) {
+                           const int* colIdx, cudaStream_t s, std::vector<int>& order,
+                           std::vector<float>* predOut) {
     std::vector<spmv_variant_t> space(variant_space(nullptr, 0));
     variant_space(space.data(), (int)space.size());
     if (mlp_inputs(model) != SPMV_NUM_FEATURES || mlp_outputs(model) != (int)space.size())
@@ -70,6 +77,7 @@ spmv_status_t learned_rank(spmv_mlp_t model, spmv_type_t type, int R, int C, int
         if (variant_applicable(space[i], R, N, maxLen)) order.push_back(i);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pred[a] < pred[b]; });
     if (order.empty()) MXS_FAIL(SPMV_ERROR_INTERNAL, "no applicable variant");
+    if (predOut) *predOut = pred;
     return SPMV_SUCCESS;
 }
 
@@ -105,13 +113,22 @@ spmv_status_t spmv_select(spmv_handle_t* h, spmv_select_mode_t mode, spmv_mlp_t 
             break;
         }
         case SPMV_SELECT_LEARNED:
-        case SPMV_SELECT_LEARNED_TOPK: {
+        case SPMV_SELECT_LEARNED_TOPK:
+        case SPMV_SELECT_LEARNED_FALLBACK: {
             if (!model) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "learned selection needs a model");
             std::vector<int> order;
-            MXS_TRY(learned_rank(model, type, R, C, N, rowPtr, colIdx, h->stream, order));
+            std::vector<float> pred;
+            MXS_TRY(learned_rank(model, type, R, C, N, rowPtr, colIdx, h->stream, order, &pred));
             idx = order[0];
-            if (mode == SPMV_SELECT_LEARNED_TOPK && topK > 1 && order.size() > 1) {
-                const int k = std::min<int>(topK, (int)order.size());
+            int k = 1;
+            if (mode == SPMV_SELECT_LEARNED_TOPK && topK > 1) k = std::min<int>(topK, (int)order.size());
+            if (mode == SPMV_SELECT_LEARNED_FALLBACK) {
+                // Low confidence: other variants predicted within kFallbackMargin
+                // of the best are timed too (at most topK, default 3).
+                const int kmax = std::min<int>(topK > 1 ? topK : 3, (int)order.size());
+                while (k < kmax && pred[order[k]] - pred[order[0]] <= kFallbackMargin) ++k;
+            }
+            if (k > 1) {
                 std::vector<spmv_variant_t> cand(k);
                 for (int i = 0; i < k; ++i) cand[i] = space[order[i]];
                 std::vector<float> ms(k);

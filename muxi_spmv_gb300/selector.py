@@ -18,7 +18,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (NUM_FEATURES, SELECT_AUTOTUNE, SELECT_HEURISTIC, SELECT_LEARNED,  # noqa: F401
-                   SELECT_LEARNED_TOPK, SPMV_TYPE_DOUBLE, SPMV_TYPE_FLOAT, GenParams, Variant, check, lib)
+                   SELECT_LEARNED_TOPK, SELECT_LEARNED_FALLBACK, FALLBACK_MARGIN, SPMV_TYPE_DOUBLE, SPMV_TYPE_FLOAT, GenParams, Variant, check, lib)
 from .api import GenSpec, SpmvHandle, _ptr, _stream_ptr, _torch
 
 DEFAULT_MODEL = Path(__file__).resolve().parent / "data" / "selector_gb300.mxsmlp"
@@ -229,4 +229,4 @@ def set_selector(handle: SpmvHandle, model: MLP | None):
 
 __all__ = ["DeviceCSR", "gen_device", "gen_device_vector", "matrix_features", "variant_space", "variant_name",
            "autotune", "MLP", "select", "set_selector", "DEFAULT_MODEL", "SELECT_HEURISTIC", "SELECT_LEARNED",
-           "SELECT_AUTOTUNE", "SELECT_LEARNED_TOPK", "NUM_FEATURES"]
+           "SELECT_AUTOTUNE", "SELECT_LEARNED_TOPK", "SELECT_LEARNED_FALLBACK", "FALLBACK_MARGIN", "NUM_FEATURES"]

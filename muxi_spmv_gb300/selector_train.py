@@ -236,6 +236,25 @@ def learned_picks(pred: np.ndarray, ms_space: np.ndarray):
     return np.where(ms_space > 0, pred, np.inf).argmin(1)
 
 
+def fallback_regrets(pred: np.ndarray, ms_space: np.ndarray, margin: float = selector.FALLBACK_MARGIN,
+                     kmax: int = 3):
+    """SELECT_LEARNED_FALLBACK on recorded times: the learned pick plus the
+    variants predicted within `margin` of it (at most kmax), fastest of them.
+    Returns (regret per matrix, candidates timed per matrix)."""
+    p = np.where(ms_space > 0, pred, np.inf)
+    order = np.argsort(p, 1, kind="stable")
+    best = np.where(ms_space > 0, ms_space, np.inf).min(1)
+    reg, cnt = np.empty(len(p)), np.empty(len(p), np.int64)
+    for r in range(len(p)):
+        o = order[r]
+        k = 1
+        while k < kmax and np.isfinite(p[r, o[k]]) and p[r, o[k]] - p[r, o[0]] <= margin:
+            k += 1
+        reg[r] = ms_space[r, o[:k]].min() / best[r] - 1.0
+        cnt[r] = k
+    return reg, cnt
+
+
 def cmd_train(a):
     import torch
     data = load_corpus(a.corpus)
@@ -291,12 +310,15 @@ def evaluate(model, data, split_name: str = "test") -> dict:
     r_heur = regrets(None, ms[sel], ms_pick=ms_all[sel, HEURISTIC_COL])
     di = default_index()
     r_def = regrets(np.full(sel.sum(), di), ms[sel])
+    r_fb, n_fb = fallback_regrets(pred, ms[sel])
     best = np.where(ms[sel] > 0, ms[sel], np.inf).argmin(1)
 
     def stats(r):
         return {"mean": float(np.mean(r)), "p95": float(np.percentile(r, 95)), "max": float(np.max(r))}
 
     return {"split": split_name, "matrices": int(sel.sum()), "learned_regret": stats(r_learn),
+            "fallback_regret": stats(r_fb), "fallback_candidates_mean": float(n_fb.mean()),
+            "fallback_timed_share": float((n_fb > 1).mean()),
             "heuristic_regret": stats(r_heur), "default_csr5_regret": stats(r_def),
             "top1_accuracy": float(np.mean(picks == best)),
             "autotune_seconds_median": float(np.median(data["meta"][sel, 6]))}
@@ -319,7 +341,7 @@ def selection_cost(model, count: int = 8, max_rows: int = 2_000_000) -> dict:
     """Wall time of spmv_select(LEARNED) vs spmv_autotune on a few matrices."""
     import torch
     h = api.SpmvHandle()
-    t_sel, t_tune = [], []
+    t_sel, t_fb, t_tune = [], [], []
     for seed in range(5, 5 + 5 * count, 5):
         spec, _, _ = spec_for_seed(seed, max_rows)
         A = selector.gen_device(spec)
@@ -331,12 +353,17 @@ def selection_cost(model, count: int = 8, max_rows: int = 2_000_000) -> dict:
         torch.cuda.synchronize()
         t_sel.append((time.perf_counter() - t0) / 10)
         t0 = time.perf_counter()
+        selector.select(h, A, selector.SELECT_LEARNED_FALLBACK, model)
+        torch.cuda.synchronize()
+        t_fb.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
         selector.autotune(h, A, None, repeats=0)
         torch.cuda.synchronize()
         t_tune.append(time.perf_counter() - t0)
         del A
     s, t = float(np.median(t_sel)), float(np.median(t_tune))
-    return {"select_ms_median": s * 1e3, "autotune_ms_median": t * 1e3, "cost_ratio": t / s}
+    return {"select_ms_median": s * 1e3, "autotune_ms_median": t * 1e3, "cost_ratio": t / s,
+            "fallback_ms_mean": float(np.mean(t_fb)) * 1e3, "fallback_cost_ratio": t / float(np.mean(t_fb))}
 
 
 def cmd_evaluate(a):

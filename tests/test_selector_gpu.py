@@ -329,6 +329,10 @@ def test_select_modes(mx, sel, cuda, handle):
     assert il == int(pred.argmin())
     vk, ik = sel.select(handle, A, sel.SELECT_LEARNED_TOPK, model, topK=3)
     assert ik in list(np.argsort(pred, kind="stable")[:3])
+    # fallback: the pick, or one of the variants predicted within the margin
+    vf, iff = sel.select(handle, A, sel.SELECT_LEARNED_FALLBACK, model)
+    near = [i for i in np.argsort(pred, kind="stable")[:3] if pred[i] - pred.min() <= sel.FALLBACK_MARGIN + 1e-6]
+    assert iff in near and space[iff].as_dict() == vf.as_dict()
     with pytest.raises(mx.SpmvError):
         sel.select(handle, A, sel.SELECT_LEARNED, None)
     with pytest.raises(mx.SpmvError):
