@@ -630,6 +630,11 @@ SPMV_API spmv_status_t spmv_select(spmv_handle_t* handle, spmv_select_mode_t mod
  * created with SPMV_KERNEL_AUTO then take the learned pick.  The handle
  * borrows the model; it must outlive the handle's use of it. */
 SPMV_API spmv_status_t spmv_set_selector(spmv_handle_t* handle, spmv_mlp_t model);
+/* How AUTO plans on this handle use the registered model:
+ * SPMV_SELECT_LEARNED (default: the model's pick, about 0.15 ms) or
+ * SPMV_SELECT_LEARNED_FALLBACK (plan creation also times the variants
+ * predicted within 2% of the pick). */
+SPMV_API spmv_status_t spmv_set_selector_mode(spmv_handle_t* handle, spmv_select_mode_t mode);
 
 /* ------------------------------------------------------------------ */
 /* Batched SpMV / SpMM over many independent FP32 CSR matrices:          */

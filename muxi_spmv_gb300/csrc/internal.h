@@ -34,6 +34,7 @@ inline unsigned grid_for(long long work, int per_block) {
 struct HandleState {
     int device = 0;
     spmv_mlp_t selector = nullptr;  // borrowed; AUTO plans consult it when set
+    spmv_select_mode_t selectorMode = SPMV_SELECT_LEARNED;  // or SPMV_SELECT_LEARNED_FALLBACK
 };
 
 // Per-device properties cached on first use (SM count, L2 size, smem).

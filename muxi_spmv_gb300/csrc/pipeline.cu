@@ -109,7 +109,7 @@ static spmv_status_t pipeline_build(spmv_handle_t* h, spmv_pipeline_t p, const i
     const size_t vs = p->type == SPMV_TYPE_FLOAT ? 4 : 8;
     const cudaStream_t hs = h->stream;
     // One variant for every slice, chosen on the whole matrix.
-    MXS_TRY(plan_variant(h, p->type, R, C, N, rowPtr, colIdx, variant, &p->variant));
+    MXS_TRY(plan_variant(h, p->type, R, C, N, rowPtr, colIdx, values, variant, &p->variant));
     for (cudaStream_t* s : {&p->sIn, &p->sOut, &p->sComp[0], &p->sComp[1]})
         MXS_CUDA(cudaStreamCreateWithFlags(s, cudaStreamNonBlocking));
 

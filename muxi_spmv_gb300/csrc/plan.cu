@@ -119,7 +119,8 @@ static spmv_status_t plan_exec(spmv_handle_t* h, spmv_plan_t p, T alpha, const T
 }
 
 spmv_status_t plan_variant(spmv_handle_t* h, spmv_type_t type, int R, int C, int N, const int* rowPtr,
-                           const int* colIdx, const spmv_variant_t* variant, spmv_variant_t* out) {
+                           const int* colIdx, const void* values, const spmv_variant_t* variant,
+                           spmv_variant_t* out) {
     *out = resolve(variant, type, R, N);
     const HandleState* hs = static_cast<const HandleState*>(h->internal);
     const bool autoPick = !variant || variant->kernel == SPMV_KERNEL_AUTO;
@@ -130,6 +131,13 @@ spmv_status_t plan_variant(spmv_handle_t* h, spmv_type_t type, int R, int C, int
         long long empties = 0;
         MXS_TRY(count_empty_rows(rowPtr, R, &empties, h->stream));
         if (empties > 0) out->itemsPerThread = 8;
+    }
+    if (autoPick && hs && hs->selector && R > 0 && N > 0 && hs->selectorMode == SPMV_SELECT_LEARNED_FALLBACK) {
+        spmv_variant_t pick{};
+        MXS_TRY(spmv_select(h, SPMV_SELECT_LEARNED_FALLBACK, hs->selector, 0, type, R, C, N, rowPtr, colIdx, values,
+                            &pick, nullptr));
+        *out = resolve(&pick, type, R, N);
+        return SPMV_SUCCESS;
     }
     if (autoPick && hs && hs->selector && R > 0 && N > 0) {
         std::vector<int> order;
@@ -171,7 +179,7 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
     p->values = values;
     p->device = h->deviceId;
     {
-        const spmv_status_t sst = plan_variant(h, type, R, C, N, rowPtr, colIdx, variant, &p->variant);
+        const spmv_status_t sst = plan_variant(h, type, R, C, N, rowPtr, colIdx, values, variant, &p->variant);
         if (sst != SPMV_SUCCESS) {
             delete p;
             return sst;

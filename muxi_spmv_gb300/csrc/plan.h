@@ -58,7 +58,8 @@ spmv_status_t learned_rank(spmv_mlp_t model, spmv_type_t type, int R, int C, int
 // The variant a plan on this matrix runs: AUTO / HEURISTIC resolved, the
 // learned pick when the handle has a selector model (plan.cu).
 spmv_status_t plan_variant(spmv_handle_t* h, spmv_type_t type, int R, int C, int N, const int* rowPtr,
-                           const int* colIdx, const spmv_variant_t* variant, spmv_variant_t* out);
+                           const int* colIdx, const void* values, const spmv_variant_t* variant,
+                           spmv_variant_t* out);
 // One SpMV of a plan on stream s (no handle; spmv_plan_exec_* without opts.sync).
 template <typename T>
 spmv_status_t plan_exec_stream(spmv_plan_t p, T alpha, const T* x, T beta, T* y, cudaStream_t s);

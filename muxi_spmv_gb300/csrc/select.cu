@@ -146,6 +146,15 @@ spmv_status_t spmv_select(spmv_handle_t* h, spmv_select_mode_t mode, spmv_mlp_t 
     return SPMV_SUCCESS;
 }
 
+spmv_status_t spmv_set_selector_mode(spmv_handle_t* h, spmv_select_mode_t mode) {
+    clear_error();
+    if (!h || !h->internal) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "handle is NULL");
+    if (mode != SPMV_SELECT_LEARNED && mode != SPMV_SELECT_LEARNED_FALLBACK)
+        MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "AUTO plans take SPMV_SELECT_LEARNED or SPMV_SELECT_LEARNED_FALLBACK");
+    static_cast<HandleState*>(h->internal)->selectorMode = mode;
+    return SPMV_SUCCESS;
+}
+
 spmv_status_t spmv_set_selector(spmv_handle_t* h, spmv_mlp_t model) {
     clear_error();
     if (!h || !h->internal) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "handle is NULL");

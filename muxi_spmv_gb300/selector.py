@@ -222,9 +222,11 @@ def select(handle: SpmvHandle, A, mode: int = SELECT_LEARNED, model: MLP | None 
     return v, idx.value
 
 
-def set_selector(handle: SpmvHandle, model: MLP | None):
-    """Makes AUTO plans on `handle` use `model` (None clears it)."""
+def set_selector(handle: SpmvHandle, model: MLP | None, mode: int = SELECT_LEARNED):
+    """Makes AUTO plans on `handle` use `model` (None clears it); mode
+    SELECT_LEARNED_FALLBACK also times the variants predicted within 2%."""
     check(lib().spmv_set_selector(handle.raw, model.raw if model is not None else None), "spmv_set_selector")
+    check(lib().spmv_set_selector_mode(handle.raw, mode), "spmv_set_selector_mode")
 
 
 __all__ = ["DeviceCSR", "gen_device", "gen_device_vector", "matrix_features", "variant_space", "variant_name",

@@ -354,6 +354,19 @@ def test_auto_plan_with_registered_selector(mx, sel, cuda):
     plan.exec(cuda.from_numpy(x).cuda(), y)
     y_ref, absum = oracle.spmv_ref(rp, ci, v, x)
     assert oracle.row_errors(host(y), y_ref, absum, tol_for(np.float32)).max() <= 1.0
+    # fallback mode: the plan's variant is one of those predicted within the margin
+    sel.set_selector(h, model, sel.SELECT_LEARNED_FALLBACK)
+    pred = host(model.forward(sel.matrix_features(A).reshape(1, -1)))[0]
+    space = sel.variant_space()
+    plan2 = mx.Plan(h, A)
+    key = lambda v: (v.kernel, v.blockSize, v.threadsPerRow, v.itemsPerThread, v.vectorWidth)
+    near = [key(space[i]) for i in np.argsort(pred, kind="stable")[:3] if pred[i] - pred[il] <= sel.FALLBACK_MARGIN + 1e-6]
+    assert key(plan2.variant) in near or key(plan2.variant) == key(vl)
+    y2 = cuda.zeros(A.numRows, device="cuda")
+    plan2.exec(cuda.from_numpy(x).cuda(), y2)
+    assert oracle.row_errors(host(y2), y_ref, absum, tol_for(np.float32)).max() <= 1.0
+    with pytest.raises(mx.SpmvError):  # AUTO plans take the learned modes only
+        mx.check(mx.lib().spmv_set_selector_mode(h.raw, sel.SELECT_AUTOTUNE), "spmv_set_selector_mode")
     sel.set_selector(h, None)
     assert mx.Plan(h, A).variant.kernel == mx.KERNEL_CSR5
     h.destroy()
