@@ -545,7 +545,7 @@ static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* ca
             // 16 four-byte or 8 eight-byte values per lane: 10 blocks (48
             // registers, 40 warps) measured best; 16 doubles need 6.
             case 128: MXS_ORDERED(128, E * sizeof(T) >= 128 ? 6 : (wide ? 10 : 16)); break;
-            case 256: MXS_ORDERED(256, wide ? 3 : 6); break;
+            case 256: MXS_ORDERED(256, E * sizeof(T) >= 128 ? 3 : (wide ? 5 : 6)); break;
             case 512: MXS_ORDERED(512, wide ? 2 : 4); break;
             case 1024: MXS_ORDERED(1024, wide ? 1 : 2); break;
             default: MXS_FAIL(SPMV_ERROR_INTERNAL, "ordered CSR5 block must be 128, 256, 512 or 1024 (got %d)", block);
