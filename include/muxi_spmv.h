@@ -231,7 +231,9 @@ typedef enum {
 /* One launch configuration of a kernel family. */
 typedef struct {
     spmv_kernel_t kernel;
-    int blockSize;       /* threads per CTA: 128, 256 or 512               */
+    int blockSize;       /* threads per CTA: SCALAR/VECTOR 64..1024 (powers
+                            of two), MERGE 128/256, CSR5 with vectorWidth
+                            32 128..1024, others 256 or 512               */
     int threadsPerRow;   /* VECTOR: 1,2,4,8,16,32; CSR5 with vectorWidth 32:
                             0 = one tile per warp; n > 0 = block ranges:
                             a block of blockSize 256/512/1024 threads owns

@@ -103,10 +103,12 @@ spmv_status_t run_rows(int block, int tpr, int vec, const RowsArgs<T>& a, cudaSt
                      (reinterpret_cast<uintptr_t>(a.values) & 15)))
         vec = 1;
     bool ok = false;
-    switch (block) {
+    switch (block) {  // the reference's family spans blocks of 64 to 1024 threads
+        case 64: ok = dispatch_tpr<T, 64>(tpr, vec, a, s); break;
         case 128: ok = dispatch_tpr<T, 128>(tpr, vec, a, s); break;
         case 256: ok = dispatch_tpr<T, 256>(tpr, vec, a, s); break;
         case 512: ok = dispatch_tpr<T, 512>(tpr, vec, a, s); break;
+        case 1024: ok = dispatch_tpr<T, 1024>(tpr, vec, a, s); break;
         default: ok = false;
     }
     if (!ok) MXS_FAIL(SPMV_ERROR_INTERNAL, "unsupported row-kernel shape block=%d tpr=%d vec=%d", block, tpr, vec);

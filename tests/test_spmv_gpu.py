@@ -62,7 +62,8 @@ VARIANTS = [("mvec", 3, 256, 8, 0, 4), ("mvec", 3, 256, 4, 0, 4), ("mvec", 3, 25
             ("merge", 3, 128, 5, 0, 1), ("merge", 3, 128, 9, 0, 1),
             ("scalar", 1, 256, 0, 1, 1), ("vec2", 2, 256, 0, 2, 1), ("vec4q", 2, 128, 0, 4, 4),
             ("vec8", 2, 512, 0, 8, 1), ("vec8q", 2, 256, 0, 8, 4), ("vec16q", 2, 256, 0, 16, 4),
-            ("vec32", 2, 256, 0, 32, 1), ("vec32q", 2, 256, 0, 32, 4), ("vec1q", 2, 256, 0, 1, 4)]
+            ("vec32", 2, 256, 0, 32, 1), ("vec32q", 2, 256, 0, 32, 4), ("vec1q", 2, 256, 0, 1, 4),
+            ("vec4", 2, 64, 0, 4, 1), ("vec2q", 2, 1024, 0, 2, 4), ("scalar", 1, 1024, 0, 1, 1)]
 
 
 def run_variant(mx, cuda, A, x, y, var, alpha, beta):
