@@ -406,6 +406,16 @@ SPMV_API spmv_status_t spmv_plan_create(spmv_handle_t* handle, spmv_type_t type,
                                int numRows, int numCols, int nnz,
                                const int* rowPtr, const int* colIdx, const void* values,
                                const spmv_variant_t* variant, spmv_plan_t* plan);
+/* Matrix ownership of a plan (the reference's CSR5Matrix borrows the CSR
+ * arrays, sparse_formats.h:351-362): SPMV_PLAN_BORROW (0, as spmv_plan_create)
+ * keeps the caller's arrays, which must outlive the plan; SPMV_PLAN_COPY
+ * copies them into memory the plan owns (synchronises the handle's stream
+ * before returning, so the caller may free its arrays). */
+#define SPMV_PLAN_BORROW 0
+#define SPMV_PLAN_COPY 1
+SPMV_API spmv_status_t spmv_plan_create_ex(spmv_handle_t* handle, spmv_type_t type, int numRows, int numCols,
+                                           int nnz, const int* rowPtr, const int* colIdx, const void* values,
+                                           const spmv_variant_t* variant, int flags, spmv_plan_t* plan);
 SPMV_API spmv_status_t spmv_plan_destroy(spmv_plan_t plan);
 /* The variant the plan runs (after AUTO / HEURISTIC resolution). */
 SPMV_API spmv_status_t spmv_plan_get_variant(spmv_plan_t plan, spmv_variant_t* variant);

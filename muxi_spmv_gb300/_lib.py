@@ -138,6 +138,7 @@ SIGNATURES = {
     "spmv_sort_columns_within_rows_f64": (S, [I, I, I, P, P, P, P]),
     "spmv_plan_create": (S, [C.POINTER(Handle), I, I, I, I, P, P, P, C.POINTER(Variant), C.POINTER(P)]),
     "spmv_plan_destroy": (S, [P]),
+    "spmv_plan_create_ex": (S, [C.POINTER(Handle), I, I, I, I, P, P, P, C.POINTER(Variant), I, C.POINTER(P)]),
     "spmv_plan_get_variant": (S, [P, C.POINTER(Variant)]),
     "spmv_plan_get_workspace_bytes": (S, [P, C.POINTER(C.c_size_t)]),
     "spmv_plan_exec_f32": (S, [C.POINTER(Handle), P, F, P, F, P]),

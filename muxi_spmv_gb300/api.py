@@ -270,13 +270,17 @@ class Plan:
     """A plan binds a device CSR matrix to one kernel variant and its
     precomputed metadata (tile coordinates, scratch)."""
 
-    def __init__(self, handle: SpmvHandle, A: CSRMatrix, variant: Variant | None = None):
+    def __init__(self, handle: SpmvHandle, A: CSRMatrix, variant: Variant | None = None, copy: bool = False):
+        """copy=True: the plan keeps its own copy of the matrix (SPMV_PLAN_COPY),
+        so A's device arrays may be freed; otherwise it borrows them."""
         self.handle = handle
-        self.A = A  # keeps the borrowed device arrays alive
+        self._f32 = _is_f32(A)
+        self.A = None if copy else A  # keeps the borrowed device arrays alive
         v = variant if variant is not None else make_variant(KERNEL_AUTO)
         p = C.c_void_p()
-        check(lib().spmv_plan_create(handle.raw, SPMV_TYPE_FLOAT if _is_f32(A) else SPMV_TYPE_DOUBLE,
-                                     *A.device_args(), C.byref(v), C.byref(p)), "spmv_plan_create")
+        check(lib().spmv_plan_create_ex(handle.raw, SPMV_TYPE_FLOAT if self._f32 else SPMV_TYPE_DOUBLE,
+                                        *A.device_args(), C.byref(v), 1 if copy else 0, C.byref(p)),
+              "spmv_plan_create_ex")
         self._p = p
 
     @property
@@ -292,7 +296,7 @@ class Plan:
         return b.value
 
     def exec(self, x, y, alpha=1.0, beta=0.0):
-        f = lib().spmv_plan_exec_f32 if _is_f32(self.A) else lib().spmv_plan_exec_f64
+        f = lib().spmv_plan_exec_f32 if self._f32 else lib().spmv_plan_exec_f64
         check(f(self.handle.raw, self._p, alpha, _ptr(x), beta, _ptr(y)), "spmv_plan_exec")
         return y
 

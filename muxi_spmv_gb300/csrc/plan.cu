@@ -371,7 +371,51 @@ spmv_status_t spmv_plan_destroy(spmv_plan_t p) {
     if (p->chainBuf) cudaFree(p->chainBuf);
     if (p->tileBits) cudaFree(p->tileBits);
     if (p->ellBuf) cudaFree(p->ellBuf);
+    if (p->ownedCsr) cudaFree(p->ownedCsr);
     delete p;
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_plan_create_ex(spmv_handle_t* h, spmv_type_t type, int R, int C, int N, const int* rowPtr,
+                                  const int* colIdx, const void* values, const spmv_variant_t* variant, int flags,
+                                  spmv_plan_t* out) {
+    clear_error();
+    if (!(flags & SPMV_PLAN_COPY)) return spmv_plan_create(h, type, R, C, N, rowPtr, colIdx, values, variant, out);
+    if (!h) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "handle is NULL");
+    if (!out) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "plan pointer is NULL");
+    if (R < 0 || C < 0 || N < 0) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "negative dimension");
+    if (type != SPMV_TYPE_FLOAT && type != SPMV_TYPE_DOUBLE)
+        MXS_FAIL(SPMV_ERROR_UNSUPPORTED_TYPE, "only SPMV_TYPE_FLOAT and SPMV_TYPE_DOUBLE are supported");
+    if (R > 0 && !rowPtr) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "rowPtr is NULL");
+    if (N > 0 && (!colIdx || !values)) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "colIdx/values is NULL");
+    // One allocation: rowPtr, colIdx and values, each 256-byte aligned.
+    const size_t vs = type == SPMV_TYPE_FLOAT ? 4 : 8;
+    const size_t a0 = (sizeof(int) * ((size_t)R + 1) + 255) & ~size_t(255);
+    const size_t a1 = (sizeof(int) * (size_t)N + 255) & ~size_t(255);
+    char* buf = nullptr;
+    MXS_CUDA(cudaMalloc(&buf, a0 + a1 + vs * (size_t)N + 256));
+    int* rp = reinterpret_cast<int*>(buf);
+    int* ci = reinterpret_cast<int*>(buf + a0);
+    void* va = buf + a0 + a1;
+    cudaError_t e = R > 0 ? cudaMemcpyAsync(rp, rowPtr, sizeof(int) * ((size_t)R + 1), cudaMemcpyDeviceToDevice,
+                                            h->stream)
+                          : cudaSuccess;
+    if (e == cudaSuccess && N > 0)
+        e = cudaMemcpyAsync(ci, colIdx, sizeof(int) * (size_t)N, cudaMemcpyDeviceToDevice, h->stream);
+    if (e == cudaSuccess && N > 0) e = cudaMemcpyAsync(va, values, vs * (size_t)N, cudaMemcpyDeviceToDevice, h->stream);
+    if (e != cudaSuccess) {
+        cudaFree(buf);
+        return cuda_fail(e, "plan matrix copy", __FILE__, __LINE__);
+    }
+    const spmv_status_t st = spmv_plan_create(h, type, R, C, N, R > 0 ? rp : nullptr, N > 0 ? ci : nullptr,
+                                              N > 0 ? va : nullptr, variant, out);
+    if (st != SPMV_SUCCESS) {
+        cudaFree(buf);
+        return st;
+    }
+    e = cudaStreamSynchronize(h->stream);  // the caller may free its arrays on return
+    (*out)->ownedCsr = buf;
+    if (e != cudaSuccess) return cuda_fail(e, "plan matrix copy", __FILE__, __LINE__);
     return SPMV_SUCCESS;
 }
 

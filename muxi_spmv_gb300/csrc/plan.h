@@ -38,6 +38,7 @@ struct spmv_plan_s {
     int* ellCol = nullptr;
     void* ellVal = nullptr;
     size_t workspaceBytes = 0;
+    void* ownedCsr = nullptr;  // SPMV_PLAN_COPY: the plan's own copy of rowPtr / colIdx / values
     // main-kernel timing (spmv_plan_profile)
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;

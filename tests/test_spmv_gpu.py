@@ -236,6 +236,27 @@ def test_plans(mx, cuda, handle, cases):
     p.destroy()
 
 
+def test_plan_copy_owns_the_matrix(mx, cuda, handle, cases):
+    """SPMV_PLAN_COPY: the plan runs from its own copy after the caller's
+    arrays are overwritten (the default borrows them)."""
+    torch = cuda
+    rp, ci, v, cols = cases["powerlaw60k"]
+    A = device_csr(mx, rp, ci, v, cols)
+    xh = mx.gen_vector(cols, 8)
+    x = torch.from_numpy(xh).cuda()
+    for var in (None, mx.make_variant(mx.KERNEL_MERGE, 256, 0, 8, 4), mx.make_variant(mx.KERNEL_VECTOR, 256, 4, 0, 4)):
+        p = mx.Plan(handle, A, var, copy=True)
+        A.d_colIdx.fill_(0)
+        A.d_values.fill_(float("nan"))
+        A.d_rowPtr.fill_(0)
+        y = torch.zeros(A.numRows, device="cuda")
+        p.exec(x, y)
+        torch.cuda.synchronize()
+        A.copyToDevice()
+        check(y, np.zeros(A.numRows, np.float32), A, xh, 1.0, 0.0)
+        p.destroy()
+
+
 def test_plan_exec_replays_from_a_cuda_graph(mx, cuda, cases):
     """A plan allocates nothing at execution and its fix-up launch (with the
     programmatic-dependent-launch attribute) captures: ten SpMVs recorded into
