@@ -700,6 +700,22 @@ SPMV_API spmv_status_t spmv_batch_exec_f32(spmv_handle_t* handle, spmv_batch_t b
                                            spmv_batch_mode_t mode);
 SPMV_API spmv_status_t spmv_batch_info(spmv_batch_t batch, long long* tiles, int* warps, long long* nnzTotal);
 
+/* Batch group: matrices with their own number of right-hand sides k[i]
+ * (1, 2, 4, 8 or 16 each).  One batch per distinct k; execution runs them
+ * back to back (the graph modes in one graph).  `variants` is NULL or 5 launch
+ * shapes, for k = 1, 2, 4, 8 and 16.  x[i] / y[i] are numCols_i x k[i] /
+ * numRows_i x k[i], row-major, as for a single batch. */
+typedef struct spmv_batch_group_s* spmv_batch_group_t;
+SPMV_API spmv_status_t spmv_batch_group_create(spmv_handle_t* handle, int count, const spmv_batch_matrix_t* mats,
+                                               const int* k, const spmv_batch_variant_t* variants,
+                                               spmv_batch_group_t* group);
+SPMV_API spmv_status_t spmv_batch_group_destroy(spmv_batch_group_t group);
+SPMV_API spmv_status_t spmv_batch_group_set_vectors_f32(spmv_batch_group_t group, const float* const* x,
+                                                        float* const* y);
+SPMV_API spmv_status_t spmv_batch_group_exec_f32(spmv_handle_t* handle, spmv_batch_group_t group, float alpha,
+                                                 float beta, spmv_batch_mode_t mode);
+SPMV_API spmv_status_t spmv_batch_group_info(spmv_batch_group_t group, int* batches, long long* nnzTotal);
+
 /* ------------------------------------------------------------------ */
 /* Host-to-host pipeline: x in pinned host memory -> y in pinned host   */
 /* memory, with the copies overlapping the SpMV.  Replaces the pinned-  */

@@ -187,6 +187,12 @@ SIGNATURES = {
     "spmv_batch_set_vectors_f32": (S, [P, C.POINTER(P), C.POINTER(P)]),
     "spmv_batch_exec_f32": (S, [C.POINTER(Handle), P, F, F, I]),
     "spmv_batch_info": (S, [P, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
+    "spmv_batch_group_create": (S, [C.POINTER(Handle), I, C.POINTER(BatchMatrix), C.POINTER(C.c_int),
+                                    C.POINTER(BatchVariant), C.POINTER(P)]),
+    "spmv_batch_group_destroy": (S, [P]),
+    "spmv_batch_group_set_vectors_f32": (S, [P, P, P]),
+    "spmv_batch_group_exec_f32": (S, [C.POINTER(Handle), P, F, F, I]),
+    "spmv_batch_group_info": (S, [P, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
     "spmv_set_selector_mode": (S, [C.POINTER(Handle), I]),
     "spmv_coo_to_csr_f32": (S, [I, I, I, P, P, P, P, P, P, P]),
     "spmv_coo_to_csr_f64": (S, [I, I, I, P, P, P, P, P, P, P]),

@@ -69,6 +69,56 @@ class BatchPlan:
             pass
 
 
+class BatchGroupPlan:
+    """Matrices with their own number of right-hand sides ks[i] (1, 2, 4, 8
+    or 16): one batch per distinct k, run back to back (one graph in the
+    graph modes).  variants: None or {k: variant dict}."""
+
+    def __init__(self, handle: SpmvHandle, mats, ks, variants: dict | None = None):
+        self.handle = handle
+        self.mats = list(mats)
+        self.ks = [int(k) for k in ks]
+        n = len(self.mats)
+        arr = (BatchMatrix * n)()
+        for i, A in enumerate(self.mats):
+            arr[i] = BatchMatrix(A.numRows, A.numCols, A.nnz, _ptr(A.d_rowPtr), _ptr(A.d_colIdx), _ptr(A.d_values))
+        karr = (C.c_int * n)(*self.ks)
+        vp = None
+        if variants:
+            va = (BatchVariant * 5)(*[BatchVariant(**variants.get(k, {})) for k in (1, 2, 4, 8, 16)])
+            vp = va
+        g = C.c_void_p()
+        check(lib().spmv_batch_group_create(handle.raw, n, arr, karr, vp, C.byref(g)), "spmv_batch_group_create")
+        self._g = g
+
+    def set_vectors(self, xs, ys):
+        n = len(self.mats)
+        xa = (C.c_void_p * n)(*[_ptr(x) for x in xs])
+        ya = (C.c_void_p * n)(*[_ptr(y) for y in ys])
+        check(lib().spmv_batch_group_set_vectors_f32(self._g, xa, ya), "spmv_batch_group_set_vectors_f32")
+        self.xs, self.ys = list(xs), list(ys)
+
+    def exec(self, alpha: float = 1.0, beta: float = 0.0, mode: int = BATCH_PERSISTENT_GRAPH):
+        check(lib().spmv_batch_group_exec_f32(self.handle.raw, self._g, alpha, beta, mode),
+              "spmv_batch_group_exec_f32")
+
+    def info(self):
+        b, n = C.c_int(), C.c_longlong()
+        check(lib().spmv_batch_group_info(self._g, C.byref(b), C.byref(n)), "spmv_batch_group_info")
+        return {"batches": b.value, "nnz": n.value}
+
+    def destroy(self):
+        if self._g:
+            check(lib().spmv_batch_group_destroy(self._g), "spmv_batch_group_destroy")
+            self._g = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
 def batch_variant_space(k: int) -> list[dict]:
     """Launch shapes the batch autotuner times for k right-hand sides."""
     out = []
@@ -157,5 +207,5 @@ def build_uneven_batch(count: int = 1024, k: int = 1, seed: int = 0, rmin: int =
     return mats, xs, ys, specs
 
 
-__all__ = ["BatchPlan", "uneven_specs", "build_uneven_batch", "batch_variant_space", "autotune_batch", "BATCH_PERSISTENT", "BATCH_PERSISTENT_GRAPH",
+__all__ = ["BatchPlan", "BatchGroupPlan", "uneven_specs", "build_uneven_batch", "batch_variant_space", "autotune_batch", "BATCH_PERSISTENT", "BATCH_PERSISTENT_GRAPH",
            "BATCH_LOOP", "BATCH_LOOP_GRAPH"]

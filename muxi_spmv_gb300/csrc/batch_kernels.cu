@@ -716,4 +716,158 @@ spmv_status_t spmv_batch_info(spmv_batch_t b, long long* tiles, int* warps, long
     return SPMV_SUCCESS;
 }
 
+// ---------------------------------------------------------------------------
+// Batch groups: matrices with their own k.  One batch per distinct k (its
+// persistent kernel is compiled for that k); execution runs the batches back
+// to back on the stream, and the graph modes capture all of them in one
+// graph.
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+struct spmv_batch_group_s {
+    int count = 0;
+    long long nnzTotal = 0;
+    std::vector<int> ks;                    // distinct k, ascending
+    std::vector<spmv_batch_t> batches;      // one per k
+    std::vector<std::vector<int>> members;  // matrix indices of each batch
+    spmv_batch_s::G graph[2];
+    cudaStream_t capStream = nullptr;
+};
+
+namespace mxs {
+namespace {
+spmv_status_t group_launch(spmv_batch_group_t g, bool loop, float alpha, float beta, cudaStream_t s) {
+    for (spmv_batch_t b : g->batches) MXS_TRY(launch_all(b, loop, alpha, beta, s));
+    return SPMV_SUCCESS;
+}
+}  // namespace
+}  // namespace mxs
+
+extern "C" {
+
+spmv_status_t spmv_batch_group_destroy(spmv_batch_group_t g) {
+    clear_error();
+    if (!g) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "batch group is NULL");
+    for (auto& gr : g->graph)
+        if (gr.exec) cudaGraphExecDestroy(gr.exec);
+    if (g->capStream) cudaStreamDestroy(g->capStream);
+    for (spmv_batch_t b : g->batches)
+        if (b) spmv_batch_destroy(b);
+    delete g;
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_batch_group_create(spmv_handle_t* h, int count, const spmv_batch_matrix_t* mats, const int* k,
+                                      const spmv_batch_variant_t* variants, spmv_batch_group_t* out) {
+    clear_error();
+    if (!h) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "handle is NULL");
+    if (!out) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "out is NULL");
+    *out = nullptr;
+    if (count <= 0 || !mats || !k) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "count must be positive, mats and k non-NULL");
+    static const int kAll[5] = {1, 2, 4, 8, 16};
+    std::vector<std::vector<int>> byK(5);
+    for (int i = 0; i < count; ++i) {
+        int j = 0;
+        while (j < 5 && kAll[j] != k[i]) ++j;
+        if (j == 5) MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "matrix %d: k must be 1, 2, 4, 8 or 16 (got %d)", i, k[i]);
+        byK[j].push_back(i);
+    }
+    spmv_batch_group_s* g = new (std::nothrow) spmv_batch_group_s();
+    if (!g) MXS_FAIL(SPMV_ERROR_MEMORY_ALLOC, "out of host memory");
+    g->count = count;
+    for (int j = 0; j < 5; ++j) {
+        if (byK[j].empty()) continue;
+        std::vector<spmv_batch_matrix_t> sub(byK[j].size());
+        for (size_t t = 0; t < sub.size(); ++t) sub[t] = mats[byK[j][t]];
+        spmv_batch_t b = nullptr;
+        const spmv_status_t st = spmv_batch_create_ex(h, (int)sub.size(), sub.data(), kAll[j],
+                                                      variants ? &variants[j] : nullptr, &b);
+        if (st != SPMV_SUCCESS) {
+            spmv_batch_group_destroy(g);
+            return st;
+        }
+        g->ks.push_back(kAll[j]);
+        g->batches.push_back(b);
+        g->members.push_back(byK[j]);
+        g->nnzTotal += b->nnzTotal;
+    }
+    *out = g;
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_batch_group_set_vectors_f32(spmv_batch_group_t g, const float* const* x, float* const* y) {
+    clear_error();
+    if (!g) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "batch group is NULL");
+    if (!x || !y) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "x/y pointer arrays are NULL");
+    for (size_t j = 0; j < g->batches.size(); ++j) {
+        std::vector<const float*> xs(g->members[j].size());
+        std::vector<float*> ys(g->members[j].size());
+        for (size_t t = 0; t < xs.size(); ++t) {
+            xs[t] = x[g->members[j][t]];
+            ys[t] = y[g->members[j][t]];
+        }
+        MXS_TRY(spmv_batch_set_vectors_f32(g->batches[j], xs.data(), ys.data()));
+    }
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_batch_group_exec_f32(spmv_handle_t* h, spmv_batch_group_t g, float alpha, float beta,
+                                        spmv_batch_mode_t mode) {
+    clear_error();
+    if (!h) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "handle is NULL");
+    if (!g) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "batch group is NULL");
+    for (spmv_batch_t b : g->batches)
+        if (!b->vectorsSet) MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "spmv_batch_group_set_vectors_f32 was not called");
+    const cudaStream_t s = h->stream;
+    switch (mode) {
+        case SPMV_BATCH_PERSISTENT:
+        case SPMV_BATCH_LOOP:
+            MXS_TRY(group_launch(g, mode == SPMV_BATCH_LOOP, alpha, beta, s));
+            break;
+        case SPMV_BATCH_PERSISTENT_GRAPH:
+        case SPMV_BATCH_LOOP_GRAPH: {
+            const bool loop = mode == SPMV_BATCH_LOOP_GRAPH;
+            auto& gr = g->graph[loop ? 1 : 0];
+            if (gr.exec && (gr.alpha != alpha || gr.beta != beta)) {
+                cudaGraphExecDestroy(gr.exec);
+                gr.exec = nullptr;
+            }
+            if (!gr.exec) {
+                if (!g->capStream) MXS_CUDA(cudaStreamCreateWithFlags(&g->capStream, cudaStreamNonBlocking));
+                cudaGraph_t graph = nullptr;
+                MXS_CUDA(cudaStreamBeginCapture(g->capStream, cudaStreamCaptureModeThreadLocal));
+                const spmv_status_t st = group_launch(g, loop, alpha, beta, g->capStream);
+                const cudaError_t e = cudaStreamEndCapture(g->capStream, &graph);
+                if (st != SPMV_SUCCESS) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return st;
+                }
+                if (e != cudaSuccess) return cuda_fail(e, "batch group graph capture", __FILE__, __LINE__);
+                const cudaError_t e2 = cudaGraphInstantiate(&gr.exec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (e2 != cudaSuccess) {
+                    gr.exec = nullptr;
+                    return cuda_fail(e2, "batch group graph instantiate", __FILE__, __LINE__);
+                }
+                gr.alpha = alpha;
+                gr.beta = beta;
+            }
+            MXS_CUDA(cudaGraphLaunch(gr.exec, s));
+            break;
+        }
+        default:
+            MXS_FAIL(SPMV_ERROR_INVALID_VECTOR, "unknown batch mode %d", (int)mode);
+    }
+    if (h->opts.sync) MXS_CUDA(cudaStreamSynchronize(s));
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_batch_group_info(spmv_batch_group_t g, int* batches, long long* nnzTotal) {
+    clear_error();
+    if (!g) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "batch group is NULL");
+    if (batches) *batches = (int)g->batches.size();
+    if (nnzTotal) *nnzTotal = g->nnzTotal;
+    return SPMV_SUCCESS;
+}
+
 }  // extern "C"

@@ -110,6 +110,47 @@ def test_batch_matches_oracle_all_modes(mx, cuda, handle, hbatch, dmats, k):
     plan.destroy()
 
 
+def test_batch_group_mixed_k_matches_oracle(mx, cuda, handle, hbatch, dmats):
+    """A group whose matrices carry their own k (all five values mixed), in
+    every mode, against the oracle column by column; the same matrices as
+    single-k batches give the same bits."""
+    from muxi_spmv_gb300 import batch as B
+    rng = np.random.default_rng(77)
+    ks = [int(k) for k in rng.choice([1, 2, 4, 8, 16], len(hbatch))]
+    X = [rng.uniform(-1, 1, c * k).astype(np.float32) for (_, _, _, c), k in zip(hbatch, ks)]
+    Y0 = [rng.uniform(-1, 1, (len(rp) - 1) * k).astype(np.float32) for (rp, *_), k in zip(hbatch, ks)]
+    dX = [cuda.from_numpy(x).cuda() if x.size else cuda.zeros(4, device="cuda") for x in X]
+    g = B.BatchGroupPlan(handle, dmats, ks)
+    assert g.info()["batches"] == len(set(ks))
+    for mode in (B.BATCH_PERSISTENT, B.BATCH_PERSISTENT_GRAPH, B.BATCH_LOOP, B.BATCH_LOOP_GRAPH):
+        dY = [cuda.from_numpy(y0.copy()).cuda() if y0.size else cuda.zeros(4, device="cuda") for y0 in Y0]
+        g.set_vectors(dX, dY)
+        g.exec(1.5, -0.5, mode)
+        cuda.cuda.synchronize()
+        Y = [y.cpu().numpy()[:y0.size] for y, y0 in zip(dY, Y0)]
+        for i, k in enumerate(ks):
+            _check([hbatch[i]], [X[i]], [Y0[i]], [Y[i]], k, 1.5, -0.5)
+    # one single-k batch of the k = 4 members reproduces their bits
+    dY = [cuda.from_numpy(y0.copy()).cuda() if y0.size else cuda.zeros(4, device="cuda") for y0 in Y0]
+    g.set_vectors(dX, dY)
+    g.exec(1.5, -0.5, B.BATCH_PERSISTENT_GRAPH)
+    cuda.cuda.synchronize()
+    Y = [y.cpu().numpy()[:y0.size] for y, y0 in zip(dY, Y0)]
+    idx = [i for i, k in enumerate(ks) if k == 4]
+    if idx:
+        p = B.BatchPlan(handle, [dmats[i] for i in idx], 4)
+        dY2 = [cuda.from_numpy(Y0[i].copy()).cuda() if Y0[i].size else cuda.zeros(4, device="cuda") for i in idx]
+        p.set_vectors([dX[i] for i in idx], dY2)
+        p.exec(1.5, -0.5, B.BATCH_PERSISTENT_GRAPH)
+        cuda.cuda.synchronize()
+        for i, y2 in zip(idx, dY2):
+            assert np.array_equal(Y[i], y2.cpu().numpy()[:Y0[i].size])
+        p.destroy()
+    with pytest.raises(mx.SpmvError):
+        B.BatchGroupPlan(handle, dmats[:2], [1, 3])
+    g.destroy()
+
+
 def test_batch_rejects_bad_input(mx, cuda, handle, dmats):
     from muxi_spmv_gb300 import batch as B
     with pytest.raises(mx.SpmvError):
