@@ -483,19 +483,40 @@ def batched_arm(args):
             o += (n + 3) // 4 * 4
         return offs, max(o, 4)
 
-    for k in [int(z) for z in args.k.split(",")]:
-        xo, xn = aligned_slices([A.numCols * k for A in mats])
-        yo, yn = aligned_slices([A.numRows * k for A in mats])
+    for kspec in args.k.split(","):
+        # "mixed": each matrix draws its own k from {1, 2, 4, 8, 16} (seeded);
+        # the batch runs as a group of single-k batches in one graph
+        mixed = kspec == "mixed"
+        if mixed:
+            kk = [int(z) for z in np.random.default_rng(4242 + rank).choice([1, 2, 4, 8, 16], len(mats))]
+            k = "mixed"
+        else:
+            k = int(kspec)
+            kk = [k] * len(mats)
+        xo, xn = aligned_slices([A.numCols * ki for A, ki in zip(mats, kk)])
+        yo, yn = aligned_slices([A.numRows * ki for A, ki in zip(mats, kk)])
         Xd = torch.empty(xn, dtype=torch.float32, device=dev)
         Yd = torch.empty(yn, dtype=torch.float32, device=dev)
-        mx.check(L.spmv_gen_device_vector_f32(xn, 1000 + k, -1.0, 1.0, Xd.data_ptr(), None), "gen x")
-        xs = [Xd[o:o + A.numCols * k] for o, A in zip(xo, mats)]
-        ys = [Yd[o:o + max(A.numRows * k, 1)] for o, A in zip(yo, mats)]
-        # launch shape picked by the batch autotuner on this batch
-        best_v, tune_ms = B.autotune_batch(h, mats, k, xs, ys, repeats=3, stream=stream)
-        plan = B.BatchPlan(h, mats, k, best_v)
+        mx.check(L.spmv_gen_device_vector_f32(xn, 1000 + (0 if mixed else k), -1.0, 1.0, Xd.data_ptr(), None),
+                 "gen x")
+        xs = [Xd[o:o + A.numCols * ki] for o, A, ki in zip(xo, mats, kk)]
+        ys = [Yd[o:o + max(A.numRows * ki, 1)] for o, A, ki in zip(yo, mats, kk)]
+        # launch shape picked by the batch autotuner on this batch (per k group)
+        if mixed:
+            best_v, tune_ms = {}, {}
+            for kg in sorted(set(kk)):
+                sel_ = [i for i, ki in enumerate(kk) if ki == kg]
+                bv, tm = B.autotune_batch(h, [mats[i] for i in sel_], kg, [xs[i] for i in sel_],
+                                          [ys[i] for i in sel_], repeats=3, stream=stream)
+                best_v[kg] = bv
+                tune_ms.update({(kg,) + key: t for key, t in tm.items()})
+            plan = B.BatchGroupPlan(h, mats, kk, best_v)
+            info = {"tiles": None, "warps": None, "groups": plan.info()["batches"]}
+        else:
+            best_v, tune_ms = B.autotune_batch(h, mats, k, xs, ys, repeats=3, stream=stream)
+            plan = B.BatchPlan(h, mats, k, best_v)
+            info = plan.info()
         plan.set_vectors(xs, ys)
-        info = plan.info()
         plan.exec(1.0, 0.0, B.BATCH_PERSISTENT_GRAPH)
         stream.synchronize()
 
@@ -506,16 +527,19 @@ def batched_arm(args):
             rp = A.d_rowPtr.cpu().numpy()
             ci = A.d_colIdx[:A.nnz].cpu().numpy()
             v = A.d_values[:A.nnz].cpu().numpy()
-            X = xs[i].cpu().numpy().reshape(A.numCols, k)
-            Y = ys[i][:A.numRows * k].cpu().numpy().reshape(A.numRows, k)
-            for j in range(k):
+            ki = kk[i]
+            X = xs[i].cpu().numpy().reshape(A.numCols, ki)
+            Y = ys[i][:A.numRows * ki].cpu().numpy().reshape(A.numRows, ki)
+            for j in range(ki):
                 yr, absum = oracle.spmv_ref(rp, ci, v, np.ascontiguousarray(X[:, j]))
                 worst = max(worst, float(oracle.row_errors(Y[:, j], yr, absum, 1e-5).max()))
                 checked += A.numRows
         if worst > 1.0:
             print(f"PARITY FAILURE k={k}: {worst}", file=sys.stderr)
 
-        nbytes = sum(A.nnz * 8 + (A.numRows + 1) * 4 + k * A.numRows * 4 + k * d * 4 for A, d in zip(mats, distinct))
+        nbytes = sum(A.nnz * 8 + (A.numRows + 1) * 4 + ki * A.numRows * 4 + ki * d * 4
+                     for A, d, ki in zip(mats, distinct, kk))
+        sumNK = sum(A.nnz * ki for A, ki in zip(mats, kk))
         times = {}
         clocks = ClockSampler(local)
         clocks.start()
@@ -539,19 +563,19 @@ def batched_arm(args):
         # the plain per-matrix loop a reference user writes: one single-matrix
         # plan per matrix (default AUTO variant), one SpMV per right-hand side
         plans = [mx.Plan(h, A) for A in mats]
-        xcols = [xs[i].view(A.numCols, k).t().contiguous() for i, A in enumerate(mats)]
-        ycols = [torch.empty(k, max(A.numRows, 1), dtype=torch.float32, device=dev) for A in mats]
+        xcols = [xs[i].view(A.numCols, kk[i]).t().contiguous() for i, A in enumerate(mats)]
+        ycols = [torch.empty(kk[i], max(A.numRows, 1), dtype=torch.float32, device=dev) for i, A in enumerate(mats)]
         plain_steps = max(2, args.steps // 8)
 
         def plain_once():
             for p_, xc, yc in zip(plans, xcols, ycols):
-                for j in range(k):
+                for j in range(xc.shape[0]):
                     p_.exec(xc[j], yc[j])
         plain_once()
         stream.synchronize()
         for i in np.linspace(0, len(mats) - 1, 4).astype(int):  # same product as the batch
             A = mats[i]
-            ref = ys[i][:A.numRows * k].view(A.numRows, k).t()
+            ref = ys[i][:A.numRows * kk[i]].view(A.numRows, kk[i]).t()
             assert torch.allclose(ycols[i][:, :A.numRows], ref, rtol=1e-4, atol=1e-4), "plain loop mismatch"
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -571,7 +595,7 @@ def batched_arm(args):
 
         def stateless_once():
             for A, xc, yc in zip(mats, xcols, ycols):
-                for j in range(k):
+                for j in range(xc.shape[0]):
                     mx.spmv_csr(A, xc[j], yc[j], 1.0, 0.0, opts)
         stateless_once()
         stream.synchronize()
@@ -611,13 +635,15 @@ def batched_arm(args):
                 "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 5),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded device generators)",
-                "config": {"workload": f"uneven{args.batch_count}", "k": k, "matrices": len(mats), "rows": sumR,
+                "config": {"workload": f"uneven{args.batch_count}", "k": k,
+                           "k_counts": {str(z): kk.count(z) for z in sorted(set(kk))} if mixed else None,
+                           "matrices": len(mats), "rows": sumR,
                            "cols": sumC, "nnz": sumN, "algorithmic_bytes": int(nbytes), "tiles": info["tiles"],
                            "warps": info["warps"], "l2": "inputs larger than L2 (no flush)",
                            "parallelism": f"replicas{ws}", "generate_s": round(gen_s, 2),
-                           "gflops": round(2 * sumN * k / (ms * 1e-3) / 1e9, 2),
+                           "gflops": round(2 * sumNK / (ms * 1e-3) / 1e9, 2),
                            "ms": {n: round(t, 4) for n, t in times.items()},
-                           "variant": best_v,
+                           "variant": {str(z): v for z, v in best_v.items()} if mixed else best_v,
                            "autotune_ms": {",".join(map(str, key)): round(t, 4) for key, t in tune_ms.items()},
                            "speedup_vs_plain_loop": round(times["plain_loop"] / ms, 3),
                            "speedup_vs_spmv_csr_loop": round(times["spmv_csr_loop"] / ms, 3),
@@ -629,12 +655,14 @@ def batched_arm(args):
                            "speedup_vs_loop_graph": round(times["loop_graph"] / ms, 3)},
                 "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                              "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                             "kernel": f"batch_tile_kernel<{k}> + batch_fixup_kernel<{k}> (graph)",
+                             "kernel": ("batch_tile_kernel<k> + batch_fixup_kernel<k> per k group (one graph)"
+                                        if mixed else f"batch_tile_kernel<{k}> + batch_fixup_kernel<{k}> (graph)"),
                              "traffic": None},
                 "e2e": {"value": round(ws * 1e3 / e2e_ms, 3), "unit": "batch/s", "h2d_bytes_per_step": int(xn * 4),
                         "d2h_bytes_per_step": int(yn * 4), "ms_per_step": round(e2e_ms, 5),
-                        "call": "spmv_batch_exec_f32 (persistent graph) with pinned X/Y copies"},
-                "gpu_launches": 2 * args.steps,
+                        "call": ("spmv_batch_group_exec_f32" if mixed else "spmv_batch_exec_f32") +
+                                " (persistent graph) with pinned X/Y copies"},
+                "gpu_launches": 2 * args.steps * (info["groups"] if mixed else 1),
                 "clocks": clocks.summary(),
                 "parity": {"matrices_checked": int(args.parity_samples), "rows_checked": checked,
                            "max_err_over_bound": worst}}
@@ -646,17 +674,17 @@ def batched_arm(args):
             for i in idx:
                 A = mats[i]
                 host.append((A.d_rowPtr.cpu().numpy(), A.d_colIdx[:A.nnz].cpu().numpy(),
-                             A.d_values[:A.nnz].cpu().numpy(), xs[i].cpu().numpy().reshape(A.numCols, k)))
-            nn = sum(int(rp[-1]) for rp, *_ in host)
+                             A.d_values[:A.nnz].cpu().numpy(), xs[i].cpu().numpy().reshape(A.numCols, kk[i])))
+            nn = sum(int(rp[-1]) * X.shape[1] for rp, _, _, X in host)  # nonzero-columns
             t = time.perf_counter()
             for rp, ci, v, X in host:
-                for j in range(k):
+                for j in range(X.shape[1]):
                     oracle.cpu_spmv(rp, ci, v, np.ascontiguousarray(X[:, j]), threads=threads)
-            cpu_s = (time.perf_counter() - t) * sumN / max(nn, 1)
+            cpu_s = (time.perf_counter() - t) * sumNK / max(nn, 1)
             line["cpu_baseline"] = {"value": round(1.0 / cpu_s, 4), "unit": "batch/s", "cores": threads,
                                     "kind": "port",
-                                    "sample": f"64 of {len(mats)} matrices ({nn} nonzeros), reference CPU loop per "
-                                              f"column, scaled to the batch's {sumN} nonzeros"}
+                                    "sample": f"64 of {len(mats)} matrices ({nn} nonzero-columns), reference CPU "
+                                              f"loop per column, scaled to the batch's {sumNK} nonzero-columns"}
         if rank == 0:
             print(json.dumps(line), flush=True)
         plan.destroy()
@@ -686,7 +714,8 @@ def main():
     ap.add_argument("--scale-rows", type=int, default=0, help="same law on this many rows (profiling cases)")
     ap.add_argument("--colperm", default="none", choices=["none", "com", "minrow", "freq"],
                     help="reorder columns first (centre of mass, the reference's min-row 'RCM', frequency)")
-    ap.add_argument("--k", default="1,2,4,8,16", help="right-hand sides (uneven batch workload)")
+    ap.add_argument("--k", default="1,2,4,8,16,mixed",
+                    help="right-hand sides (uneven batch workload); 'mixed': each matrix draws its own k")
     ap.add_argument("--batch-count", type=int, default=1024, help="matrices (uneven batch workload)")
     ap.add_argument("--parity-samples", type=int, default=8, help="matrices checked (uneven batch workload)")
     args = ap.parse_args()
