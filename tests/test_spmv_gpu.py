@@ -236,6 +236,43 @@ def test_plans(mx, cuda, handle, cases):
     p.destroy()
 
 
+def test_unused_nonfinite_x_does_not_leak(mx, cuda, handle):
+    """Padding slots and masked lanes read x[0] or other columns without using
+    them: an Inf / NaN in columns no nonzero references must not reach y."""
+    torch = cuda
+    rng = np.random.default_rng(31)
+    lens = np.r_[rng.integers(1, 9, 3000), 700, rng.integers(1, 6, 2000)].astype(np.int32)
+    rp = np.r_[0, np.cumsum(lens)].astype(np.int32)
+    cols = 6000
+    ci = np.concatenate([np.sort(rng.choice(np.arange(2, cols), l, replace=False)) for l in lens]).astype(np.int32)
+    v = rng.standard_normal(rp[-1]).astype(np.float32)
+    assert rp[-1] % 512 != 0  # a partial last tile
+    A = device_csr(mx, rp, ci, v, cols)
+    xh = mx.gen_vector(cols, 3)
+    xh[0], xh[1] = np.inf, np.nan  # columns 0 and 1 are never referenced
+    x = torch.from_numpy(xh).cuda()
+    y_ref, _ = oracle.spmv_ref(rp, ci, v, xh)
+    assert np.isfinite(y_ref).all()
+    variants = [None, mx.make_variant(mx.KERNEL_CSR5, 128, 0, 4, 32), mx.make_variant(mx.KERNEL_CSR5, 256, 0, 8, 1),
+                mx.make_variant(mx.KERNEL_MERGE, 256, 0, 8, 4), mx.make_variant(mx.KERNEL_MERGE, 128, 0, 9),
+                mx.make_variant(mx.KERNEL_VECTOR, 256, 8, 0, 4), mx.make_variant(mx.KERNEL_SCALAR, 128),
+                mx.make_variant(mx.KERNEL_ELL), mx.make_variant(mx.KERNEL_BAND, 256, 0, 8)]
+    for var in variants:
+        try:
+            p = mx.Plan(handle, A, var)
+        except mx.SpmvError:
+            continue  # a shape this matrix does not take (ELL padding gate)
+        y = torch.zeros(A.numRows, device="cuda")
+        p.exec(x, y)
+        torch.cuda.synchronize()
+        assert torch.isfinite(y).all(), var.as_dict() if var is not None else "auto"
+        p.destroy()
+    y = torch.zeros(A.numRows, device="cuda")
+    mx.spmv_csr(A, x, y)
+    torch.cuda.synchronize()
+    assert torch.isfinite(y).all()
+
+
 def test_plan_copy_owns_the_matrix(mx, cuda, handle, cases):
     """SPMV_PLAN_COPY: the plan runs from its own copy after the caller's
     arrays are overwritten (the default borrows them)."""
