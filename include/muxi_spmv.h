@@ -20,6 +20,12 @@
  *   tests/test_row_reordering.cu:99-143, tests/test_combined_optimizations.cu:176-181
  *   tests/test_column_reordering.cu:116-199  row / "RCM" / frequency reorders
  *   src/generators/matrix_generator.h:19-102  synthetic matrix generators
+ *   src/generators/mtx_io.h:22-85     Matrix Market reader / writer
+ *   src/formats/sparse_formats.h:113-162  COOMatrix (declared there, no kernel)
+ *   src/spmv/csr/spmv_csr.cuh:105-107, src/api/spmv_api.h:70-78  transpose SpMV
+ *   tests/test_pinned_memory.cu:245-380  host-memory SpMV (pipelines here)
+ *   tests/test_multi_stream.cu:121-236   multi-stream SpMV (batches here)
+ * and adds plans, the learned kernel selector and batched SpMV / SpMM.
  *
  * Threading: a handle is not thread safe (same as the reference).  All device
  * work is asynchronous on the stream given (opts->stream or the handle's
