@@ -198,6 +198,30 @@ SPMV_API spmv_status_t spmv_coo_f64(int numRows, int numCols, int nnz, const int
                                     const double* values, const double* x, double* y, double alpha, double beta,
                                     const spmv_opts_t* opts);
 
+/* BSR (src/formats/sparse_formats.h:207-269, BSRMatrix: declared there
+ * without a conversion or kernel), block size B = 2, 4 or 8, blocks dense
+ * B x B row-major, numBlockRows = ceil(numRows / B).  Conversion from a CSR
+ * whose columns are sorted within rows, in two calls:
+ * spmv_csr_to_bsr_count fills bRowPtr[numBlockRows + 1] and returns the block
+ * count (synchronises the stream; unsorted rows give
+ * SPMV_ERROR_INVALID_MATRIX); spmv_csr_to_bsr_* then fills bColIdx[numBlocks]
+ * and bValues[numBlocks * B * B] (entries of one row at the same column add).
+ * spmv_bsr_*: y = alpha*A*x + beta*y. */
+SPMV_API spmv_status_t spmv_csr_to_bsr_count(int numRows, int numCols, int nnz, const int* rowPtr, const int* colIdx,
+                                             int B, int* bRowPtr, int* numBlocks, cudaStream_t stream);
+SPMV_API spmv_status_t spmv_csr_to_bsr_f32(int numRows, int numCols, int nnz, const int* rowPtr, const int* colIdx,
+                                           const float* values, int B, const int* bRowPtr, int* bColIdx,
+                                           float* bValues, cudaStream_t stream);
+SPMV_API spmv_status_t spmv_csr_to_bsr_f64(int numRows, int numCols, int nnz, const int* rowPtr, const int* colIdx,
+                                           const double* values, int B, const int* bRowPtr, int* bColIdx,
+                                           double* bValues, cudaStream_t stream);
+SPMV_API spmv_status_t spmv_bsr_f32(int numRows, int numCols, int B, int numBlockRows, const int* bRowPtr,
+                                    const int* bColIdx, const float* bValues, const float* x, float* y, float alpha,
+                                    float beta, cudaStream_t stream);
+SPMV_API spmv_status_t spmv_bsr_f64(int numRows, int numCols, int B, int numBlockRows, const int* bRowPtr,
+                                    const int* bColIdx, const double* bValues, const double* x, double* y,
+                                    double alpha, double beta, cudaStream_t stream);
+
 /* FP32 CSR SpMV that allocates no device memory (no counterpart in the
  * reference).  Same kernels and results as spmv_csr_f32 (default merge-path
  * variant), for callers that cannot allocate: code recording a CUDA graph,

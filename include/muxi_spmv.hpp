@@ -223,10 +223,11 @@ struct COOMatrix {
     }
 };
 
-// CSR2Matrix<T> (sparse_formats.h:164-205) and BSRMatrix<T, B>
-// (sparse_formats.h:207-269): declared by the reference without kernels or
-// conversions; the same members here, so code naming them compiles.
-// spmv_exec refuses both formats (SPMV_ERROR_UNSUPPORTED_FORMAT).
+// CSR2Matrix<T> (sparse_formats.h:164-205): declared by the reference without
+// a kernel or conversion; the same members here, so code naming it compiles;
+// spmv_exec refuses it (SPMV_ERROR_UNSUPPORTED_FORMAT).  BSRMatrix<T, B>
+// (sparse_formats.h:207-269): the same members, filled on the device by
+// csr_to_bsr<T, B> (B = 2, 4 or 8) and run by spmv_bsr<T, B> / spmv_exec.
 template <typename FloatType>
 struct CSR2Matrix {
     int numRows = 0, numCols = 0, nnz = 0;
@@ -252,6 +253,22 @@ struct BSRMatrix {
     FloatType* d_values = nullptr;
     bool ownsHostMemory = false;
     bool ownsDeviceMemory = false;
+
+    BSRMatrix() = default;
+    BSRMatrix(const BSRMatrix&) = delete;
+    BSRMatrix& operator=(const BSRMatrix&) = delete;
+    ~BSRMatrix() {
+        if (ownsHostMemory) {
+            std::free(rowPtr);
+            std::free(colIdx);
+            std::free(values);
+        }
+        if (ownsDeviceMemory) {
+            cudaFree(d_rowPtr);
+            cudaFree(d_colIdx);
+            cudaFree(d_values);
+        }
+    }
 };
 
 template <typename FloatType>
@@ -400,10 +417,58 @@ spmv_status_t spmv_ellpack(const ELLPACKMatrix<FloatType>& ellpack, const FloatT
     return ell_call(ellpack, d_x, d_y, stream);
 }
 
+// CSR -> BSR on the device (columns sorted within rows); the BSR owns its
+// device arrays.
+template <typename FloatType, int BlockSize>
+spmv_status_t csr_to_bsr(const CSRMatrix<FloatType>& csr, BSRMatrix<FloatType, BlockSize>& bsr,
+                         cudaStream_t stream = 0) {
+    static_assert(BlockSize == 2 || BlockSize == 4 || BlockSize == 8, "block size 2, 4 or 8");
+    bsr.numRows = csr.numRows;
+    bsr.numCols = csr.numCols;
+    bsr.numBlockRows = (csr.numRows + BlockSize - 1) / BlockSize;
+    bsr.numBlockCols = (csr.numCols + BlockSize - 1) / BlockSize;
+    if (cudaMalloc(&bsr.d_rowPtr, sizeof(int) * ((size_t)bsr.numBlockRows + 1)) != cudaSuccess)
+        return SPMV_ERROR_MEMORY_ALLOC;
+    bsr.ownsDeviceMemory = true;
+    spmv_status_t st = spmv_csr_to_bsr_count(csr.numRows, csr.numCols, csr.nnz, csr.d_rowPtr, csr.d_colIdx, BlockSize,
+                                             bsr.d_rowPtr, &bsr.numBlocks, stream);
+    if (st != SPMV_SUCCESS) return st;
+    const size_t nb = (size_t)(bsr.numBlocks > 0 ? bsr.numBlocks : 1);
+    if (cudaMalloc(&bsr.d_colIdx, sizeof(int) * nb) != cudaSuccess ||
+        cudaMalloc(&bsr.d_values, sizeof(FloatType) * nb * BlockSize * BlockSize) != cudaSuccess)
+        return SPMV_ERROR_MEMORY_ALLOC;
+    if (std::is_same<FloatType, float>::value)
+        return spmv_csr_to_bsr_f32(csr.numRows, csr.numCols, csr.nnz, csr.d_rowPtr, csr.d_colIdx,
+                                   reinterpret_cast<const float*>(csr.d_values), BlockSize, bsr.d_rowPtr, bsr.d_colIdx,
+                                   reinterpret_cast<float*>(bsr.d_values), stream);
+    return spmv_csr_to_bsr_f64(csr.numRows, csr.numCols, csr.nnz, csr.d_rowPtr, csr.d_colIdx,
+                               reinterpret_cast<const double*>(csr.d_values), BlockSize, bsr.d_rowPtr, bsr.d_colIdx,
+                               reinterpret_cast<double*>(bsr.d_values), stream);
+}
+
+namespace detail {
+template <typename FloatType>
+inline spmv_status_t bsr_call(int R, int C, int B, int nbr, const int* rp, const int* ci, const FloatType* v,
+                              const FloatType* x, FloatType* y, FloatType alpha, FloatType beta, cudaStream_t s) {
+    if (std::is_same<FloatType, float>::value)
+        return spmv_bsr_f32(R, C, B, nbr, rp, ci, reinterpret_cast<const float*>(v), reinterpret_cast<const float*>(x),
+                            reinterpret_cast<float*>(y), (float)alpha, (float)beta, s);
+    return spmv_bsr_f64(R, C, B, nbr, rp, ci, reinterpret_cast<const double*>(v), reinterpret_cast<const double*>(x),
+                        reinterpret_cast<double*>(y), (double)alpha, (double)beta, s);
+}
+}  // namespace detail
+
+template <typename FloatType, int BlockSize>
+spmv_status_t spmv_bsr(const BSRMatrix<FloatType, BlockSize>& bsr, const FloatType* x, FloatType* y,
+                       cudaStream_t stream = 0, FloatType alpha = 1, FloatType beta = 0) {
+    return detail::bsr_call<FloatType>(bsr.numRows, bsr.numCols, BlockSize, bsr.numBlockRows, bsr.d_rowPtr,
+                                       bsr.d_colIdx, bsr.d_values, x, y, alpha, beta, stream);
+}
+
 // spmv_exec<T> (spmv_api.h:57-65, declared but not defined by the reference):
-// `matrix` points to a CSRMatrix<T>, CSR5Matrix<T>, COOMatrix<T> or
-// ELLPACKMatrix<T> according to `format`; runs on the handle's stream and
-// options.  CSR2 and BSR are refused.
+// `matrix` points to a CSRMatrix<T>, CSR5Matrix<T>, COOMatrix<T>,
+// BSRMatrix<T, B> or ELLPACKMatrix<T> according to `format`; runs on the
+// handle's stream and options.  CSR2 is refused.
 template <typename FloatType>
 spmv_status_t spmv_exec(spmv_handle_t* handle, spmv_format_t format, const void* matrix, const FloatType* x,
                         FloatType* y, FloatType alpha = 1.0, FloatType beta = 0.0) {
@@ -416,6 +481,12 @@ spmv_status_t spmv_exec(spmv_handle_t* handle, spmv_format_t format, const void*
             return spmv_csr<FloatType>(*static_cast<const CSRMatrix<FloatType>*>(matrix), x, y, alpha, beta, o);
         case SPMV_FORMAT_CSR5:
             return spmv_csr5<FloatType>(*static_cast<const CSR5Matrix<FloatType>*>(matrix), x, y, alpha, beta, o);
+        case SPMV_FORMAT_BSR: {
+            // every BSRMatrix<T, B> has the same layout; blockSize gives B
+            const auto& b = *static_cast<const BSRMatrix<FloatType, 2>*>(matrix);
+            return detail::bsr_call<FloatType>(b.numRows, b.numCols, b.blockSize, b.numBlockRows, b.d_rowPtr,
+                                               b.d_colIdx, b.d_values, x, y, alpha, beta, handle->stream);
+        }
         case SPMV_FORMAT_COO: {
             const auto& c = *static_cast<const COOMatrix<FloatType>*>(matrix);
             if (std::is_same<FloatType, float>::value)

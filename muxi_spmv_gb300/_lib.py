@@ -194,6 +194,11 @@ SIGNATURES = {
     "spmv_batch_group_exec_f32": (S, [C.POINTER(Handle), P, F, F, I]),
     "spmv_batch_group_info": (S, [P, C.POINTER(C.c_int), C.POINTER(C.c_longlong)]),
     "spmv_set_selector_mode": (S, [C.POINTER(Handle), I]),
+    "spmv_csr_to_bsr_count": (S, [I, I, I, P, P, I, P, C.POINTER(C.c_int), P]),
+    "spmv_csr_to_bsr_f32": (S, [I, I, I, P, P, P, I, P, P, P, P]),
+    "spmv_csr_to_bsr_f64": (S, [I, I, I, P, P, P, I, P, P, P, P]),
+    "spmv_bsr_f32": (S, [I, I, I, I, P, P, P, P, P, F, F, P]),
+    "spmv_bsr_f64": (S, [I, I, I, I, P, P, P, P, P, D, D, P]),
     "spmv_coo_to_csr_f32": (S, [I, I, I, P, P, P, P, P, P, P]),
     "spmv_coo_to_csr_f64": (S, [I, I, I, P, P, P, P, P, P, P]),
     "spmv_coo_f32": (S, [I, I, I, P, P, P, P, P, F, F, C.POINTER(Opts)]),

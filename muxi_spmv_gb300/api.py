@@ -199,6 +199,44 @@ def spmv_coo(A: COOMatrix, x, y, alpha=1.0, beta=0.0, opts: Opts | None = None):
     return y
 
 
+class BSRMatrix:
+    """BSRMatrix<T, B> (src/formats/sparse_formats.h:207-269) on the device:
+    d_rowPtr (block rows + 1), d_colIdx (block columns), d_values (dense
+    B x B blocks, row-major)."""
+
+    def __init__(self, numRows: int, numCols: int, blockSize: int, numBlocks: int, d_rowPtr, d_colIdx, d_values):
+        self.numRows, self.numCols, self.blockSize, self.numBlocks = numRows, numCols, blockSize, numBlocks
+        self.numBlockRows = (numRows + blockSize - 1) // blockSize
+        self.numBlockCols = (numCols + blockSize - 1) // blockSize
+        self.d_rowPtr, self.d_colIdx, self.d_values = d_rowPtr, d_colIdx, d_values
+
+
+def csr_to_bsr(A: CSRMatrix, blockSize: int, stream=None) -> BSRMatrix:
+    """Device BSR of a CSR matrix whose columns are sorted within rows."""
+    torch = _torch()
+    dev = A.d_values.device
+    B = int(blockSize)
+    nbr = (A.numRows + B - 1) // B
+    rp = torch.empty(nbr + 1, dtype=torch.int32, device=dev)
+    nb = C.c_int()
+    check(lib().spmv_csr_to_bsr_count(A.numRows, A.numCols, A.nnz, _ptr(A.d_rowPtr), _ptr(A.d_colIdx), B, _ptr(rp),
+                                      C.byref(nb), _stream_ptr(stream)), "spmv_csr_to_bsr_count")
+    ci = torch.empty(max(nb.value, 1), dtype=torch.int32, device=dev)
+    va = torch.empty(max(nb.value * B * B, 1), dtype=A.d_values.dtype, device=dev)
+    f = lib().spmv_csr_to_bsr_f32 if _is_f32(A) else lib().spmv_csr_to_bsr_f64
+    check(f(*A.device_args(), B, _ptr(rp), _ptr(ci), _ptr(va), _stream_ptr(stream)), "spmv_csr_to_bsr")
+    return BSRMatrix(A.numRows, A.numCols, B, nb.value, rp, ci, va)
+
+
+def spmv_bsr(M: BSRMatrix, x, y, alpha=1.0, beta=0.0, stream=None):
+    """y = alpha*A*x + beta*y for a BSR matrix."""
+    torch = _torch()
+    f = lib().spmv_bsr_f32 if M.d_values.dtype == torch.float32 else lib().spmv_bsr_f64
+    check(f(M.numRows, M.numCols, M.blockSize, M.numBlockRows, _ptr(M.d_rowPtr), _ptr(M.d_colIdx), _ptr(M.d_values),
+            _ptr(x), _ptr(y), alpha, beta, _stream_ptr(stream)), "spmv_bsr")
+    return y
+
+
 def spmv_csr_transpose(A: CSRMatrix, x, y, alpha=1.0, beta=0.0, stream=None):
     """y = alpha*A^T*x + beta*y (the reference's spmv_exec_transpose, spmv_api.h:70-78)."""
     o = spmv_default_opts(stream)

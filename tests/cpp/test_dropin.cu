@@ -173,9 +173,9 @@ int main() {
         cudaMemcpy(y.data(), dy, m * sizeof(float), cudaMemcpyDeviceToHost);
         report("spmv_exec COO", status == SPMV_SUCCESS && close(y, want, scale));
     }
-    report("spmv_exec CSR2 / BSR unsupported",
-           spmv_exec<float>(handle, SPMV_FORMAT_CSR2, &A, dx, dy) == SPMV_ERROR_UNSUPPORTED_FORMAT &&
-               spmv_exec<float>(handle, SPMV_FORMAT_BSR, &A, dx, dy) == SPMV_ERROR_UNSUPPORTED_FORMAT);
+    // BSR (sparse_formats.h:207-269) from the column-sorted copy B below
+    report("spmv_exec CSR2 unsupported",
+           spmv_exec<float>(handle, SPMV_FORMAT_CSR2, &A, dx, dy) == SPMV_ERROR_UNSUPPORTED_FORMAT);
 
     // spmv_exec_transpose (spmv_api.h:70-78): y = A^T x.
     {
@@ -212,6 +212,23 @@ int main() {
     for (int r = 0; r < m && sorted; ++r)
         for (int j = B.rowPtr[r]; j + 1 < B.rowPtr[r + 1] && sorted; ++j) sorted = B.colIdx[j] <= B.colIdx[j + 1];
     report("sortColumnsWithinRows", sorted);
+
+    // BSR of the column-sorted B (dx still holds the reordered x): spmv_bsr and spmv_exec
+    B.copyToDevice();
+    {
+        BSRMatrix<float, 4> bsr;
+        status = csr_to_bsr<float, 4>(B, bsr);
+        bool ok = status == SPMV_SUCCESS && bsr.numBlockRows == (m + 3) / 4 && bsr.numBlocks > 0;
+        cudaMemset(dy, 0, m * sizeof(float));
+        ok = ok && spmv_bsr<float, 4>(bsr, dx, dy) == SPMV_SUCCESS;
+        fetch();
+        report("csr_to_bsr + spmv_bsr", ok && close(y, want, scale));
+        cudaMemset(dy, 0, m * sizeof(float));
+        status = spmv_exec<float>(handle, SPMV_FORMAT_BSR, &bsr, dx, dy);
+        cudaStreamSynchronize(st);
+        cudaMemcpy(y.data(), dy, m * sizeof(float), cudaMemcpyDeviceToHost);
+        report("spmv_exec BSR", status == SPMV_SUCCESS && close(y, want, scale));
+    }
 
     // Matrix Market round trip through muxi_spmv::io (src/generators/mtx_io.h).
     {
