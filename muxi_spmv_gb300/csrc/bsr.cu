@@ -106,14 +106,41 @@ bsr_kernel(int R, int C, int nbr, const int* __restrict__ bRowPtr, const int* __
     static_assert(B == 2 || B == 4 || B == 8, "32 lanes cover whole blocks");
     const int slot = EB <= 32 ? lane / EB : 0;
     const int e0 = EB <= 32 ? lane % EB : lane;  // element of the block (row-major)
-    for (int b = b0 + slot; b < b1; b += SLOTS) {
+    // Four block steps at a time: their loads and gathers are in flight together.
+    constexpr int U = 4;
+    int b = b0 + slot;
+    for (; b + (U - 1) * SLOTS < b1; b += U * SLOTS) {
+        int bc[U];
+        T v[U][PER], g[U][PER];
+#pragma unroll
+        for (int u = 0; u < U; ++u) bc[u] = __ldg(bColIdx + b + u * SLOTS);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int q = 0; q < PER; ++q) v[u][q] = ld_stream(bValues + (size_t)(b + u * SLOTS) * EB + e0 + 32 * q);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+                const int col = bc[u] * B + (e0 + 32 * q) % B;
+                g[u][q] = ld_x(x + (col < C ? col : 0));  // padding columns past C hold zeros
+            }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+                const int col = bc[u] * B + (e0 + 32 * q) % B;
+                acc[q] += col < C ? v[u][q] * g[u][q] : T(0);
+            }
+    }
+    for (; b < b1; b += SLOTS) {
         const int bc = __ldg(bColIdx + b);
 #pragma unroll
         for (int q = 0; q < PER; ++q) {
             const int e = e0 + 32 * q;
             const int col = bc * B + e % B;
             const T v = ld_stream(bValues + (size_t)b * EB + e);
-            const T g = ld_x(x + (col < C ? col : 0));  // padding columns past C hold zeros
+            const T g = ld_x(x + (col < C ? col : 0));
             acc[q] += col < C ? v * g : T(0);
         }
     }
