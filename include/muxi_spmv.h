@@ -456,6 +456,16 @@ SPMV_API spmv_status_t spmv_plan_exec_f32(spmv_handle_t* handle, spmv_plan_t pla
 SPMV_API spmv_status_t spmv_plan_exec_f64(spmv_handle_t* handle, spmv_plan_t plan, double alpha,
                                  const double* x, double beta, double* y);
 
+/* y = alpha*op(A)*x + beta*y with op = SPMV_OP_NORMAL (as spmv_plan_exec_*)
+ * or SPMV_OP_TRANSPOSE (x: numRows entries, y: numCols).  The transpose is
+ * built from the matrix's values on the first transposed call and kept with
+ * the plan (a caller that changes the values recreates the plan).
+ * SPMV_OP_CONJUGATE: SPMV_ERROR_UNSUPPORTED_FORMAT. */
+SPMV_API spmv_status_t spmv_plan_exec_op_f32(spmv_handle_t* handle, spmv_plan_t plan, spmv_operation_t op,
+                                             float alpha, const float* x, float beta, float* y);
+SPMV_API spmv_status_t spmv_plan_exec_op_f64(spmv_handle_t* handle, spmv_plan_t plan, spmv_operation_t op,
+                                             double alpha, const double* x, double beta, double* y);
+
 /* Device-side failure word of a plan.  The pipelined BAND kernel never waits
  * without a bound: a wait that gives up (about 2 s) raises this word and the
  * kernel returns.  Synchronises; *code = 0 when clean, else the raised code

@@ -143,6 +143,8 @@ SIGNATURES = {
     "spmv_plan_get_workspace_bytes": (S, [P, C.POINTER(C.c_size_t)]),
     "spmv_plan_exec_f32": (S, [C.POINTER(Handle), P, F, P, F, P]),
     "spmv_plan_exec_f64": (S, [C.POINTER(Handle), P, D, P, D, P]),
+    "spmv_plan_exec_op_f32": (S, [C.POINTER(Handle), P, I, F, P, F, P]),
+    "spmv_plan_exec_op_f64": (S, [C.POINTER(Handle), P, I, D, P, D, P]),
     "spmv_plan_device_error": (S, [P, C.POINTER(C.c_int)]),
     "spmv_plan_profile": (S, [P, I]),
     "spmv_plan_profile_read": (S, [P, C.POINTER(C.c_double), C.POINTER(C.c_int)]),

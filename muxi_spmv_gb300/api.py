@@ -333,7 +333,14 @@ class Plan:
         check(lib().spmv_plan_get_workspace_bytes(self._p, C.byref(b)), "spmv_plan_get_workspace_bytes")
         return b.value
 
-    def exec(self, x, y, alpha=1.0, beta=0.0):
+    def exec(self, x, y, alpha=1.0, beta=0.0, transpose: bool = False):
+        """y = alpha*A*x + beta*y, or alpha*A^T*x + beta*y with transpose=True
+        (A^T is built on the first such call and kept)."""
+        if transpose:
+            f = lib().spmv_plan_exec_op_f32 if self._f32 else lib().spmv_plan_exec_op_f64
+            check(f(self.handle.raw, self._p, _lib.SPMV_OP_TRANSPOSE, alpha, _ptr(x), beta, _ptr(y)),
+                  "spmv_plan_exec_op")
+            return y
         f = lib().spmv_plan_exec_f32 if self._f32 else lib().spmv_plan_exec_f64
         check(f(self.handle.raw, self._p, alpha, _ptr(x), beta, _ptr(y)), "spmv_plan_exec")
         return y

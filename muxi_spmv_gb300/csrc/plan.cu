@@ -372,6 +372,8 @@ spmv_status_t spmv_plan_destroy(spmv_plan_t p) {
     if (p->tileBits) cudaFree(p->tileBits);
     if (p->ellBuf) cudaFree(p->ellBuf);
     if (p->ownedCsr) cudaFree(p->ownedCsr);
+    if (p->tPlan) spmv_plan_destroy(p->tPlan);
+    if (p->tBuf) cudaFree(p->tBuf);
     delete p;
     return SPMV_SUCCESS;
 }
@@ -436,6 +438,58 @@ spmv_status_t spmv_plan_get_workspace_bytes(spmv_plan_t p, size_t* bytes) {
 spmv_status_t spmv_plan_exec_f32(spmv_handle_t* h, spmv_plan_t p, float alpha, const float* x, float beta,
                                  float* y) {
     return plan_exec<float>(h, p, alpha, x, beta, y);
+}
+
+}  // extern "C"
+
+namespace mxs {
+// op = SPMV_OP_TRANSPOSE: y = alpha*A^T*x + beta*y through a plan of A^T
+// built (csr_transpose, AUTO variant) on the first such call and kept.
+template <typename T>
+static spmv_status_t plan_exec_op(spmv_handle_t* h, spmv_plan_t p, spmv_operation_t op, T alpha, const T* x, T beta,
+                                  T* y) {
+    clear_error();
+    if (!h) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "handle is NULL");
+    if (!p) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "plan is NULL");
+    if (op == SPMV_OP_NORMAL) return plan_exec<T>(h, p, alpha, x, beta, y);
+    if (op != SPMV_OP_TRANSPOSE) MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "SPMV_OP_CONJUGATE is not supported");
+    const spmv_type_t want = sizeof(T) == 4 ? SPMV_TYPE_FLOAT : SPMV_TYPE_DOUBLE;
+    if (p->type != want) MXS_FAIL(SPMV_ERROR_UNSUPPORTED_TYPE, "plan value type does not match the call");
+    if (!p->tPlan) {
+        const int R = p->numRows, C = p->numCols, N = p->nnz;
+        const size_t a = (sizeof(int) * ((size_t)C + 1) + 255) & ~size_t(255);
+        const size_t b = (sizeof(int) * (size_t)(N > 0 ? N : 1) + 255) & ~size_t(255);
+        char* buf = nullptr;
+        MXS_CUDA(cudaMalloc(&buf, a + b + sizeof(T) * (size_t)(N > 0 ? N : 1)));
+        int* tRp = reinterpret_cast<int*>(buf);
+        int* tCi = reinterpret_cast<int*>(buf + a);
+        T* tVa = reinterpret_cast<T*>(buf + a + b);
+        spmv_status_t st = csr_transpose<T>(R, C, N, p->rowPtr, p->colIdx, static_cast<const T*>(p->values), tRp,
+                                            tCi, tVa, h->stream);
+        spmv_plan_t q = nullptr;
+        if (st == SPMV_SUCCESS)
+            st = spmv_plan_create(h, p->type, C, R, N, C > 0 ? tRp : nullptr, N > 0 ? tCi : nullptr,
+                                  N > 0 ? static_cast<const void*>(tVa) : nullptr, nullptr, &q);
+        if (st != SPMV_SUCCESS) {
+            cudaFree(buf);
+            return st;
+        }
+        p->tPlan = q;
+        p->tBuf = buf;
+    }
+    return plan_exec<T>(h, p->tPlan, alpha, x, beta, y);
+}
+}  // namespace mxs
+
+extern "C" {
+
+spmv_status_t spmv_plan_exec_op_f32(spmv_handle_t* h, spmv_plan_t p, spmv_operation_t op, float alpha,
+                                    const float* x, float beta, float* y) {
+    return plan_exec_op<float>(h, p, op, alpha, x, beta, y);
+}
+spmv_status_t spmv_plan_exec_op_f64(spmv_handle_t* h, spmv_plan_t p, spmv_operation_t op, double alpha,
+                                    const double* x, double beta, double* y) {
+    return plan_exec_op<double>(h, p, op, alpha, x, beta, y);
 }
 spmv_status_t spmv_plan_exec_f64(spmv_handle_t* h, spmv_plan_t p, double alpha, const double* x, double beta,
                                  double* y) {

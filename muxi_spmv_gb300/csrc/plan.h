@@ -39,6 +39,9 @@ struct spmv_plan_s {
     void* ellVal = nullptr;
     size_t workspaceBytes = 0;
     void* ownedCsr = nullptr;  // SPMV_PLAN_COPY: the plan's own copy of rowPtr / colIdx / values
+    // SPMV_OP_TRANSPOSE executions: A^T built on first use, with its own plan
+    spmv_plan_s* tPlan = nullptr;
+    void* tBuf = nullptr;
     // main-kernel timing (spmv_plan_profile)
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;

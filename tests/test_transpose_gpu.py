@@ -86,3 +86,49 @@ def test_transpose_is_deterministic(mx, cuda, mats):
         mx.spmv_csr_transpose(A, x, y)
         ys.append(y.cpu().numpy())
     assert all(np.array_equal(ys[0], b) for b in ys[1:])
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_plan_transpose_matches_oracle(mx, cuda, mats, dtype):
+    """A plan answers both y = A x and y = A^T x; the transposed plan is built
+    on the first transposed call and reused afterwards."""
+    h = mx.spmv_create_handle()
+    for name, (rp, ci, v, cols) in mats.items():
+        rows = len(rp) - 1
+        v = v.astype(dtype)
+        A = device_csr(mx, rp, ci, v, cols)
+        plan = mx.Plan(h, A)
+        xh = mx.gen_vector(rows, 33, dtype=dtype)
+        trp, tci, tv = np_transpose(rp, ci, v, cols)
+        y_ref, absum = oracle.spmv_ref(trp, tci, tv, xh)
+        x = cuda.from_numpy(xh).cuda() if rows else cuda.zeros(1, dtype=cuda.float32 if dtype == np.float32
+                                                             else cuda.float64, device="cuda")
+        for alpha, beta in ((1.0, 0.0), (-2.0, 0.5), (1.0, 0.0)):
+            y0 = mx.gen_vector(cols, 9, dtype=dtype)
+            y = cuda.from_numpy(y0.copy()).cuda() if cols else x.new_zeros(1)
+            plan.exec(x, y, alpha, beta, transpose=True)
+            cuda.cuda.synchronize()
+            got = y.cpu().numpy()[:cols].astype(np.float64)
+            want = alpha * y_ref + beta * y0.astype(np.float64)
+            bound = tol_for(dtype) * (abs(alpha) * absum + abs(beta * y0.astype(np.float64)))
+            assert (np.abs(got - want) <= bound + (0 if dtype == np.float64 else 1e-30)).all(), (name, alpha)
+        # the plan still answers A x after the transposed calls
+        xn = mx.gen_vector(cols, 34, dtype=dtype)
+        yn_ref, absum_n = oracle.spmv_ref(rp, ci, v, xn)
+        xd = cuda.from_numpy(xn).cuda() if cols else x.new_zeros(1)
+        yd = x.new_zeros(max(rows, 1))
+        plan.exec(xd, yd)
+        cuda.cuda.synchronize()
+        got = yd.cpu().numpy()[:rows].astype(np.float64)
+        assert (np.abs(got - yn_ref) <= tol_for(dtype) * absum_n + (0 if dtype == np.float64 else 1e-30)).all(), name
+
+
+def test_plan_refuses_conjugate(mx, cuda, mats):
+    rp, ci, v, cols = mats["poisson"]
+    A = device_csr(mx, rp, ci, v, cols)
+    h = mx.spmv_create_handle()
+    plan = mx.Plan(h, A)
+    x = cuda.zeros(len(rp) - 1, device="cuda")
+    y = cuda.zeros(cols, device="cuda")
+    st = mx.lib().spmv_plan_exec_op_f32(h.raw, plan._p, 2, 1.0, x.data_ptr(), 0.0, y.data_ptr())  # SPMV_OP_CONJUGATE
+    assert st == -7
