@@ -64,14 +64,16 @@ __device__ __forceinline__ void csr5_load(Csr5Load<T, E>& L, long long t, int la
     }
 }
 
-// The row logic of a tile over this lane's E products p[e] = a_j * x[col_j]
-// (zero past the tile end); RP(r): rowPtr[r] for r in [0, rLast+1].
+// The row logic of a tile over this lane's E nonzeros: acc(run, e) adds the
+// lane's e-th term a_j * x[col_j] to the running row sum (called only for
+// positions before the tile end); RP(r): rowPtr[r] for r in [0, rLast+1].
 // noEmpty: the caller knows every row holds a nonzero (no empty-row pass).
-template <typename T, int E, typename RowPtrAt>
-__device__ __forceinline__ void csr5_tile_rows(const T (&p)[E], int rFirst, int rLast, long long t, int lane, int nnz,
+// plain: alpha = 1 and beta = 0 (y takes the sums as they are).
+template <typename T, int E, typename Acc, typename RowPtrAt>
+__device__ __forceinline__ void csr5_tile_rows(Acc acc, int rFirst, int rLast, long long t, int lane, int nnz,
                                                T* __restrict__ y, T alpha, T beta, bool bz,
                                                int* __restrict__ carryRow, T* __restrict__ carryVal, RowPtrAt RP,
-                                               bool noEmpty = false) {
+                                               bool noEmpty = false, bool plain = false) {
     // 32-bit positions: the plans that run these tiles require
     // nnz <= INT_MAX - 32*E*32, so no position below overflows.
     constexpr int SIGMA = 32 * E;
@@ -112,7 +114,7 @@ __device__ __forceinline__ void csr5_tile_rows(const T (&p)[E], int rFirst, int 
                         headRow = key;
                         headVal = run;
                     } else {
-                        y[key] = axpby(alpha, run, beta, bz, y + key);
+                        y[key] = axpbyp(plain, alpha, run, beta, bz, y + key);
                     }
                     do {
                         ++key;
@@ -120,7 +122,7 @@ __device__ __forceinline__ void csr5_tile_rows(const T (&p)[E], int rFirst, int 
                     } while (j >= rowEnd);
                     run = T(0);
                 }
-                run += p[e];
+                run = acc(run, e);
             }
         }
     }
@@ -136,8 +138,8 @@ __device__ __forceinline__ void csr5_tile_rows(const T (&p)[E], int rFirst, int 
     const T prevIncl = __shfl_up_sync(kFull, incl, 1);
     if (!has) return;
     const T cin = (lane > 0 && prevKey == startRow) ? prevIncl : T(0);
-    if (headRow >= 0) y[headRow] = axpby(alpha, headVal + cin, beta, bz, y + headRow);
-    if (rowEnd == laneEnd) y[key] = axpby(alpha, incl, beta, bz, y + key);  // tail row ends in this lane
+    if (headRow >= 0) y[headRow] = axpbyp(plain, alpha, headVal + cin, beta, bz, y + headRow);
+    if (rowEnd == laneEnd) y[key] = axpbyp(plain, alpha, incl, beta, bz, y + key);  // tail row ends in this lane
     if (laneEnd == tEnd) {  // the lane holding the tile's last nonzero
         carryRow[t] = rowEnd > laneEnd ? key : -1;
         carryVal[t] = incl;
@@ -157,7 +159,8 @@ __device__ __forceinline__ void csr5_tile_core(const int (&cIdx)[E], const T (&v
     T p[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) p[e] = j0 + e < laneEnd ? vals[e] * gather(cIdx[e]) : T(0);
-    csr5_tile_rows<T, E>(p, rFirst, rLast, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal, RP);
+    csr5_tile_rows<T, E>([&](T r, int e) { return r + p[e]; }, rFirst, rLast, t, lane, nnz, y, alpha, beta, bz,
+                         carryRow, carryVal, RP);
 }
 
 // Tile with register-loaded data (csr5_load): stages the rowPtr slice in this

@@ -127,6 +127,16 @@ __device__ __forceinline__ T axpby(T alpha, T s, T beta, bool beta_zero, const T
     return beta_zero ? alpha * s : alpha * s + beta * (*yp);
 }
 
+// axpby that stores s itself when `plain` (alpha = 1 and beta = 0, decided on
+// the host: 1*s == s exactly).  GB300 runs FP64 arithmetic at about 1.25
+// TFLOP/s per GPU, a small fraction of its FP32 rate, so the FP64 kernels keep
+// such instructions -- the alpha == 1 test included -- off the plain y = A x
+// path.
+template <typename T>
+__device__ __forceinline__ T axpbyp(bool plain, T alpha, T s, T beta, bool beta_zero, const T* yp) {
+    return plain ? s : axpby(alpha, s, beta, beta_zero, yp);
+}
+
 // Sum over aligned groups of G lanes (G a power of two <= 32).
 template <int G, typename T>
 __device__ __forceinline__ T group_sum(T v) {

@@ -58,10 +58,11 @@ csr5_tile_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int
 // rFirst plus the set bits up to its first position (a popcount prefix over
 // the words); a set bit inside the lane closes the current row.  Same
 // results as csr5_tile_rows, without reading rowPtr.
-template <typename T, int E>
-__device__ __forceinline__ void csr5_tile_rows_bits(const T (&p)[E], unsigned word, int rFirst, long long t, int lane,
+template <typename T, int E, typename Acc>
+__device__ __forceinline__ void csr5_tile_rows_bits(Acc acc, unsigned word, int rFirst, long long t, int lane,
                                                     int nnz, T* __restrict__ y, T alpha, T beta, bool bz,
-                                                    int* __restrict__ carryRow, T* __restrict__ carryVal) {
+                                                    int* __restrict__ carryRow, T* __restrict__ carryVal,
+                                                    bool plain) {
     constexpr int SIGMA = 32 * E;
     const int tStart = (int)t * SIGMA;
     const int tEnd = min(tStart + SIGMA, nnz);
@@ -98,12 +99,12 @@ __device__ __forceinline__ void csr5_tile_rows_bits(const T (&p)[E], unsigned wo
                         headRow = key;
                         headVal = run;
                     } else {
-                        y[key] = axpby(alpha, run, beta, bz, y + key);
+                        y[key] = axpbyp(plain, alpha, run, beta, bz, y + key);
                     }
                     ++key;
                     run = T(0);
                 }
-                run += p[e];
+                run = acc(run, e);
             }
         }
     }
@@ -121,8 +122,8 @@ __device__ __forceinline__ void csr5_tile_rows_bits(const T (&p)[E], unsigned wo
     const T prevIncl = __shfl_up_sync(kFull, incl2, 1);
     if (!has) return;
     const T cin = (lane > 0 && prevKey == startRow) ? prevIncl : T(0);
-    if (headRow >= 0) y[headRow] = axpby(alpha, headVal + cin, beta, bz, y + headRow);
-    if (endsHere) y[key] = axpby(alpha, incl2, beta, bz, y + key);
+    if (headRow >= 0) y[headRow] = axpbyp(plain, alpha, headVal + cin, beta, bz, y + headRow);
+    if (endsHere) y[key] = axpbyp(plain, alpha, incl2, beta, bz, y + key);
     if (laneEnd == tEnd) {  // the lane holding the tile's last nonzero
         carryRow[t] = endsHere ? -1 : key;
         carryVal[t] = incl2;
@@ -221,13 +222,47 @@ __device__ __forceinline__ void csr5_ordered_load(OrderedLoad<T, E>& L, long lon
     L.rLast = t + 1 < tiles ? __ldg(tileRow + t + 1) : numRows - 1;
 }
 
+// Hands this lane's E consecutive terms to the row logic `rows(acc)`.  FP32:
+// the products go through shared memory (one round trip).  FP64: the values,
+// then the gathered x, go through the same region and each term is one FMA
+// -- on GB300 the FP64 pipe, not memory, bounds an FP64 SpMV, and a product
+// plus an add cost it two instructions per nonzero where the FMA costs one.
+template <typename T, int E, typename Rows>
+__device__ __forceinline__ void ordered_handoff(const T (&v)[E], const T (&g)[E], int lane, T* sP, Rows rows) {
+    if constexpr (sizeof(T) == 8) {
+        T a[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) sP[ordered_slot<T, E>(lane + 32 * e)] = v[e];
+        __syncwarp();
+#pragma unroll
+        for (int e = 0; e < E; ++e) a[e] = sP[ordered_slot<T, E>(lane * E + e)];
+        __syncwarp();
+#pragma unroll
+        for (int e = 0; e < E; ++e) sP[ordered_slot<T, E>(lane + 32 * e)] = g[e];
+        __syncwarp();
+        rows([&](T r, int e) { return fma(a[e], sP[ordered_slot<T, E>(lane * E + e)], r); });
+    } else {
+#pragma unroll
+        for (int e = 0; e < E; ++e) sP[ordered_slot<T, E>(lane + 32 * e)] = v[e] * g[e];
+        __syncwarp();
+        T p[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) p[e] = sP[ordered_slot<T, E>(lane * E + e)];
+        rows([&](T r, int e) { return r + p[e]; });
+    }
+}
+
+// betaZero value of the ordered kernels when alpha = 1 and beta = 0 (1: beta
+// = 0 only), so that no thread tests alpha in FP64.
+constexpr int kPlainAxpby = 3;
+
 // REUSE: the warp runs further tiles on the same shared regions afterwards.
 template <typename T, int E, bool REUSE>
 __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L, long long t, int lane, int nnz,
                                                      const int* __restrict__ rowPtr, const T* __restrict__ x,
                                                      T* __restrict__ y, T alpha, T beta, bool bz, long long tiles,
                                                      int* __restrict__ carryRow, T* __restrict__ carryVal,
-                                                     bool noEmpty, int* sRp, T* sP, bool useBits) {
+                                                     bool noEmpty, int* sRp, T* sP, bool useBits, bool plain) {
     const int rFirst = L.rFirst, rLast = L.rLast;
     T g[E];
 #pragma unroll
@@ -248,13 +283,10 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
     }
 
     if (useBits) {
-#pragma unroll
-        for (int e = 0; e < E; ++e) sP[ordered_slot<T, E>(lane + 32 * e)] = L.v[e] * g[e];
-        __syncwarp();
-        T p[E];
-#pragma unroll
-        for (int e = 0; e < E; ++e) p[e] = sP[ordered_slot<T, E>(lane * E + e)];
-        csr5_tile_rows_bits<T, E>(p, L.bits, rFirst, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal);
+        ordered_handoff<T, E>(L.v, g, lane, sP, [&](auto acc) {
+            csr5_tile_rows_bits<T, E>(acc, L.bits, rFirst, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal,
+                                      plain);
+        });
         if (REUSE) __syncwarp();
         return;
     }
@@ -267,15 +299,11 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
             if (i < nRp) sRp[i] = __ldg(rowPtr + rFirst + i);
         }
     }
-#pragma unroll
-    for (int e = 0; e < E; ++e) sP[ordered_slot<T, E>(lane + 32 * e)] = L.v[e] * g[e];
-    __syncwarp();
-    T p[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) p[e] = sP[ordered_slot<T, E>(lane * E + e)];
-    csr5_tile_rows<T, E>(p, rFirst, rLast, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal,
-                         [&](int r) { return (staged && r >= rFirst) ? sRp[r - rFirst] : __ldg(rowPtr + r); },
-                         noEmpty);
+    ordered_handoff<T, E>(L.v, g, lane, sP, [&](auto acc) {
+        csr5_tile_rows<T, E>(acc, rFirst, rLast, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal,
+                             [&](int r) { return (staged && r >= rFirst) ? sRp[r - rFirst] : __ldg(rowPtr + r); },
+                             noEmpty, plain);
+    });
     if (REUSE) __syncwarp();  // the regions are reused by this warp's next tile
 }
 
@@ -286,11 +314,12 @@ __device__ __forceinline__ void csr5_ordered_tile(long long t, int lane, int num
                                                   T* __restrict__ y, T alpha, T beta, bool bz,
                                                   const int* __restrict__ tileRow, long long tiles,
                                                   int* __restrict__ carryRow, T* __restrict__ carryVal, bool noEmpty,
-                                                  const unsigned* __restrict__ tileBits, int* sRp, T* sP) {
+                                                  const unsigned* __restrict__ tileBits, int* sRp, T* sP,
+                                                  bool plain) {
     OrderedLoad<T, E> L;
     csr5_ordered_load<T, E>(L, t, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
     csr5_ordered_compute<T, E, false>(L, t, lane, nnz, rowPtr, x, y, alpha, beta, bz, tiles, carryRow, carryVal,
-                                      noEmpty, sRp, sP, tileBits != nullptr);
+                                      noEmpty, sRp, sP, tileBits != nullptr, plain);
 }
 
 // One tile per warp, BLOCK threads per block, MINB resident blocks per SM
@@ -312,7 +341,7 @@ csr5_ordered_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const 
     const int w = threadIdx.x >> 5;
     csr5_ordered_tile<T, E>(t, threadIdx.x & 31, numRows, nnz, rowPtr, colIdx, values, x, y, alpha, beta,
                             betaZero != 0, tileRow, tiles, carryRow, carryVal, noEmptyRows != 0, tileBits, sRpAll[w],
-                            sPAll[w]);
+                            sPAll[w], betaZero == kPlainAxpby);
 }
 
 // Block ranges: block b owns the `perBlock` consecutive tiles from
@@ -348,7 +377,7 @@ csr5_ordered_range_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, 
         if (lane == 0) next = atomicAdd(&sNext, 1);
         csr5_ordered_compute<T, E, true>(L, t, lane, nnz, rowPtr, x, y, alpha, beta, betaZero != 0, tiles,
                                          carryRow, carryVal, noEmptyRows != 0, sRpAll[w], sPAll[w],
-                                         tileBits != nullptr);
+                                         tileBits != nullptr, betaZero == kPlainAxpby);
         t = __shfl_sync(0xffffffffu, next, 0);
     }
 }
@@ -535,16 +564,18 @@ csr5_fixup_kernel(long long tiles, const int* __restrict__ carryRow, const T* __
 template <typename T, int E>
 static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* carryRow, T* carryVal,
                                     const RowsArgs<T>& a, int block, int chunk, const unsigned* bits, cudaStream_t s) {
+    const int bzFlags = a.betaZero ? (a.alpha == T(1) ? kPlainAxpby : 1) : 0;
     if (chunk <= 0) {
         constexpr bool wide = E * sizeof(T) >= 64;  // 16 doubles or floats per lane: fewer, larger blocks
 #define MXS_ORDERED(B, M)                                                                                        \
     csr5_ordered_kernel<T, E, B, M><<<grid_for(tiles * 32, B), B, 0, s>>>(                                        \
-        a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha, a.beta, a.betaZero, tileRow, tiles,   \
+        a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha, a.beta, bzFlags, tileRow, tiles,   \
         carryRow, carryVal, a.noEmptyRows, bits)
         switch (block) {
             // 16 four-byte or 8 eight-byte values per lane: 10 blocks (48
-            // registers, 40 warps) measured best; 16 doubles need 6.
-            case 128: MXS_ORDERED(128, E * sizeof(T) >= 128 ? 6 : (wide ? 10 : 16)); break;
+            // registers, 40 warps) measured best; 16 doubles (the FP64 FMA
+            // hand-off holds a lane's 16 values) fit 96 registers at 5.
+            case 128: MXS_ORDERED(128, E * sizeof(T) >= 128 ? 5 : (wide ? 10 : 16)); break;
             case 256: MXS_ORDERED(256, E * sizeof(T) >= 128 ? 3 : (wide ? 5 : 6)); break;
             case 512: MXS_ORDERED(512, wide ? 2 : 4); break;
             case 1024: MXS_ORDERED(1024, wide ? 1 : 2); break;
@@ -559,7 +590,7 @@ static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* ca
     if (per > 0x7fffffffLL) MXS_FAIL(SPMV_ERROR_INTERNAL, "CSR5 block range too large");
 #define MXS_RANGE(B, M)                                                                                          \
     csr5_ordered_range_kernel<T, E, B, M><<<grid_for(tiles, (int)per), B, 0, s>>>(                                \
-        a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha, a.beta, a.betaZero, tileRow, tiles,   \
+        a.numRows, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y, a.alpha, a.beta, bzFlags, tileRow, tiles,   \
         carryRow, carryVal, a.noEmptyRows, (int)per, bits)
     switch (block) {
         case 256: MXS_RANGE(256, wide ? 3 : 8); break;
