@@ -128,8 +128,11 @@ __device__ __forceinline__ void csr5_tile_rows(Acc acc, int rFirst, int rLast, l
     }
 
     T incl = run;
+    // FP64: stop at the longest run of lanes sharing a key (keys rise with the lane)
+    const int span = sizeof(T) == 8 ? key_run_length(key, lane) : 32;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
+        if (off >= span) break;  // warp-uniform
         const int k2 = __shfl_up_sync(kFull, key, off);
         const T v2 = __shfl_up_sync(kFull, incl, off);
         if (lane >= off && k2 == key) incl += v2;

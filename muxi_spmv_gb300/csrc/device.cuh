@@ -137,6 +137,15 @@ __device__ __forceinline__ T axpbyp(bool plain, T alpha, T s, T beta, bool beta_
     return plain ? s : axpby(alpha, s, beta, beta_zero, yp);
 }
 
+// Longest run of lanes sharing `key`, for keys non-decreasing over the lanes:
+// a segmented inclusive scan over such keys is complete after the steps
+// with offsets below this length (integer work only; the FP64 adds of the
+// skipped steps are what the FP64 kernels save).
+__device__ __forceinline__ int key_run_length(int key, int lane) {
+    const unsigned same = __match_any_sync(kFull, key);
+    return __reduce_max_sync(kFull, (unsigned)(lane - (__ffs(same) - 1) + 1));
+}
+
 // Sum over aligned groups of G lanes (G a power of two <= 32).
 template <int G, typename T>
 __device__ __forceinline__ T group_sum(T v) {

@@ -112,8 +112,11 @@ __device__ __forceinline__ void csr5_tile_rows_bits(Acc acc, unsigned word, int 
     const bool endsHere = laneEnd == tEnd ? endsAtTileEnd : (lane < 31 && nextFirst != 0u);
 
     T incl2 = run;
+    // FP64: stop at the longest run of lanes sharing a key (keys rise with the lane)
+    const int span = sizeof(T) == 8 ? key_run_length(key, lane) : 32;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
+        if (off >= span) break;  // warp-uniform
         const int k2 = __shfl_up_sync(kFull, key, off);
         const T v2 = __shfl_up_sync(kFull, incl2, off);
         if (lane >= off && k2 == key) incl2 += v2;
