@@ -466,6 +466,25 @@ SPMV_API spmv_status_t spmv_plan_exec_op_f32(spmv_handle_t* handle, spmv_plan_t 
 SPMV_API spmv_status_t spmv_plan_exec_op_f64(spmv_handle_t* handle, spmv_plan_t plan, spmv_operation_t op,
                                              double alpha, const double* x, double beta, double* y);
 
+/* The conversion and execute calls of a format-generic ABI (the
+ * reference's csr5_preprocess + spmv_csr5, csr_to_ellpack + spmv_ellpack and
+ * its declared-only spmv_exec, src/api/spmv_api.h:57-65, as one pair).
+ * spmv_convert builds a plan of the CSR arrays in `format`:
+ *   SPMV_FORMAT_CSR   any CSR kernel (`params`: a variant; NULL: AUTO);
+ *   SPMV_FORMAT_CSR5  CSR5 tiles (`params`: blockSize / itemsPerThread =
+ *                     sigma/32 / vectorWidth 32 for nonzero-order gathers;
+ *                     NULL: the default tile shape);
+ *   SPMV_FORMAT_ELL   column-major ELLPACK (refused beyond 2x padding).
+ * Other formats: SPMV_ERROR_UNSUPPORTED_FORMAT (COO and BSR have their own
+ * conversions above).  spmv_exec_* = spmv_plan_exec_op_*. */
+SPMV_API spmv_status_t spmv_convert(spmv_handle_t* handle, spmv_type_t type, int numRows, int numCols, int nnz,
+                                    const int* rowPtr, const int* colIdx, const void* values, spmv_format_t format,
+                                    const spmv_variant_t* params, spmv_plan_t* plan);
+SPMV_API spmv_status_t spmv_exec_f32(spmv_handle_t* handle, spmv_plan_t plan, spmv_operation_t op, float alpha,
+                                     const float* x, float beta, float* y);
+SPMV_API spmv_status_t spmv_exec_f64(spmv_handle_t* handle, spmv_plan_t plan, spmv_operation_t op, double alpha,
+                                     const double* x, double beta, double* y);
+
 /* Device-side failure word of a plan.  The pipelined BAND kernel never waits
  * without a bound: a wait that gives up (about 2 s) raises this word and the
  * kernel returns.  Synchronises; *code = 0 when clean, else the raised code

@@ -24,6 +24,7 @@ STATUS_NAMES = {
 
 SPMV_TYPE_FLOAT, SPMV_TYPE_DOUBLE = 0, 1
 SPMV_OP_NORMAL, SPMV_OP_TRANSPOSE = 0, 1
+SPMV_FORMAT_CSR, SPMV_FORMAT_COO, SPMV_FORMAT_CSR2, SPMV_FORMAT_BSR, SPMV_FORMAT_CSR5, SPMV_FORMAT_ELL = 0, 1, 2, 3, 4, 5
 
 KERNEL_AUTO, KERNEL_SCALAR, KERNEL_VECTOR, KERNEL_MERGE, KERNEL_CSR5, KERNEL_ELL, KERNEL_HEURISTIC, \
     KERNEL_BAND = range(8)
@@ -144,6 +145,9 @@ SIGNATURES = {
     "spmv_plan_exec_f32": (S, [C.POINTER(Handle), P, F, P, F, P]),
     "spmv_plan_exec_f64": (S, [C.POINTER(Handle), P, D, P, D, P]),
     "spmv_plan_exec_op_f32": (S, [C.POINTER(Handle), P, I, F, P, F, P]),
+    "spmv_convert": (S, [C.POINTER(Handle), I, I, I, I, P, P, P, I, C.POINTER(Variant), C.POINTER(P)]),
+    "spmv_exec_f32": (S, [C.POINTER(Handle), P, I, F, P, F, P]),
+    "spmv_exec_f64": (S, [C.POINTER(Handle), P, I, D, P, D, P]),
     "spmv_plan_exec_op_f64": (S, [C.POINTER(Handle), P, I, D, P, D, P]),
     "spmv_plan_device_error": (S, [P, C.POINTER(C.c_int)]),
     "spmv_plan_profile": (S, [P, I]),

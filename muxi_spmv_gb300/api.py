@@ -17,7 +17,9 @@ from . import _lib
 from ._lib import (GenParams, Opts, SpmvError, Variant, check, lib, KERNEL_AUTO, KERNEL_SCALAR,  # noqa: F401
                    KERNEL_BAND,
                    KERNEL_VECTOR, KERNEL_MERGE, KERNEL_CSR5, KERNEL_ELL, KERNEL_HEURISTIC,
-                   SPMV_TYPE_FLOAT, SPMV_TYPE_DOUBLE)
+                   SPMV_TYPE_FLOAT, SPMV_TYPE_DOUBLE, SPMV_OP_NORMAL, SPMV_OP_TRANSPOSE,
+                   SPMV_FORMAT_CSR, SPMV_FORMAT_COO, SPMV_FORMAT_CSR2, SPMV_FORMAT_BSR, SPMV_FORMAT_CSR5,
+                   SPMV_FORMAT_ELL)
 
 
 def _torch():
@@ -321,6 +323,18 @@ class Plan:
               "spmv_plan_create_ex")
         self._p = p
 
+    @classmethod
+    def from_format(cls, handle: SpmvHandle, A: CSRMatrix, fmt: int, params: Variant | None = None) -> "Plan":
+        """spmv_convert: a plan of A in SPMV_FORMAT_CSR / _CSR5 / _ELL (borrows A)."""
+        self = cls.__new__(cls)
+        self.handle, self._f32, self.A = handle, _is_f32(A), A
+        p = C.c_void_p()
+        check(lib().spmv_convert(handle.raw, SPMV_TYPE_FLOAT if self._f32 else SPMV_TYPE_DOUBLE, *A.device_args(),
+                                 int(fmt), C.byref(params) if params is not None else None, C.byref(p)),
+              "spmv_convert")
+        self._p = p
+        return self
+
     @property
     def variant(self) -> Variant:
         v = Variant()
@@ -343,6 +357,12 @@ class Plan:
             return y
         f = lib().spmv_plan_exec_f32 if self._f32 else lib().spmv_plan_exec_f64
         check(f(self.handle.raw, self._p, alpha, _ptr(x), beta, _ptr(y)), "spmv_plan_exec")
+        return y
+
+    def exec_op(self, op: int, x, y, alpha=1.0, beta=0.0):
+        """spmv_exec_*: y = alpha*op(A)*x + beta*y, op = SPMV_OP_NORMAL / SPMV_OP_TRANSPOSE."""
+        f = lib().spmv_exec_f32 if self._f32 else lib().spmv_exec_f64
+        check(f(self.handle.raw, self._p, int(op), alpha, _ptr(x), beta, _ptr(y)), "spmv_exec")
         return y
 
     def device_error(self) -> int:

@@ -483,6 +483,56 @@ static spmv_status_t plan_exec_op(spmv_handle_t* h, spmv_plan_t p, spmv_operatio
 
 extern "C" {
 
+spmv_status_t spmv_convert(spmv_handle_t* h, spmv_type_t type, int R, int C, int N, const int* rowPtr,
+                           const int* colIdx, const void* values, spmv_format_t format,
+                           const spmv_variant_t* params, spmv_plan_t* out) {
+    clear_error();
+    if (out) *out = nullptr;
+    spmv_variant_t v{};
+    switch (format) {
+        case SPMV_FORMAT_CSR:  // any CSR kernel; NULL: AUTO
+            if (params) v = *params;
+            else v.kernel = SPMV_KERNEL_AUTO;
+            break;
+        case SPMV_FORMAT_CSR5:  // CSR5 tiles; NULL: the default tile shape
+            if (params) {
+                v = *params;
+                v.kernel = SPMV_KERNEL_CSR5;
+            } else {
+                v = resolve(nullptr, type, R, N);
+                if (v.kernel != SPMV_KERNEL_CSR5) {
+                    v = spmv_variant_t{};
+                    v.kernel = SPMV_KERNEL_CSR5;
+                    v.blockSize = 128;
+                    v.itemsPerThread = 8;
+                    v.vectorWidth = 32;
+                }
+                if (h && v.itemsPerThread == 16 && R > 0 && rowPtr) {  // as AUTO: 256-nonzero tiles with empty rows
+                    long long empties = 0;
+                    MXS_TRY(count_empty_rows(rowPtr, R, &empties, h->stream));
+                    if (empties > 0) v.itemsPerThread = 8;
+                }
+            }
+            break;
+        case SPMV_FORMAT_ELL:  // column-major ELLPACK; refused beyond 2x padding
+            v.kernel = SPMV_KERNEL_ELL;
+            break;
+        default:
+            MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT,
+                     "spmv_convert builds CSR, CSR5 or ELL plans (COO: spmv_coo_to_csr_*; BSR: spmv_csr_to_bsr_*)");
+    }
+    return spmv_plan_create(h, type, R, C, N, rowPtr, colIdx, values, &v, out);
+}
+
+spmv_status_t spmv_exec_f32(spmv_handle_t* h, spmv_plan_t p, spmv_operation_t op, float alpha, const float* x,
+                            float beta, float* y) {
+    return plan_exec_op<float>(h, p, op, alpha, x, beta, y);
+}
+spmv_status_t spmv_exec_f64(spmv_handle_t* h, spmv_plan_t p, spmv_operation_t op, double alpha, const double* x,
+                            double beta, double* y) {
+    return plan_exec_op<double>(h, p, op, alpha, x, beta, y);
+}
+
 spmv_status_t spmv_plan_exec_op_f32(spmv_handle_t* h, spmv_plan_t p, spmv_operation_t op, float alpha,
                                     const float* x, float beta, float* y) {
     return plan_exec_op<float>(h, p, op, alpha, x, beta, y);

@@ -132,3 +132,50 @@ def test_plan_refuses_conjugate(mx, cuda, mats):
     y = cuda.zeros(cols, device="cuda")
     st = mx.lib().spmv_plan_exec_op_f32(h.raw, plan._p, 2, 1.0, x.data_ptr(), 0.0, y.data_ptr())  # SPMV_OP_CONJUGATE
     assert st == -7
+
+
+@pytest.mark.parametrize("fmt", ["CSR", "CSR5", "ELL"])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_convert_and_exec(mx, cuda, mats, fmt, dtype):
+    """spmv_convert builds a plan in the named format; spmv_exec runs it for
+    op = NORMAL and TRANSPOSE (the same bounds against the oracle)."""
+    h = mx.spmv_create_handle()
+    f = getattr(mx, "SPMV_FORMAT_" + fmt)
+    for name, (rp, ci, v, cols) in mats.items():
+        rows = len(rp) - 1
+        if fmt == "ELL" and rows and np.diff(rp).max(initial=0) * rows > 2 * max(len(ci), 1):
+            with pytest.raises(mx.SpmvError) as e:
+                mx.Plan.from_format(h, device_csr(mx, rp, ci, v.astype(dtype), cols), f)
+            assert e.value.status == -7, name
+            continue
+        v = v.astype(dtype)
+        A = device_csr(mx, rp, ci, v, cols)
+        plan = mx.Plan.from_format(h, A, f)
+        if fmt == "CSR5":
+            assert plan.variant.kernel == mx.KERNEL_CSR5
+        if fmt == "ELL":
+            assert plan.variant.kernel == mx.KERNEL_ELL
+        zero = cuda.zeros(1, dtype=cuda.float32 if dtype == np.float32 else cuda.float64, device="cuda")
+        for op, n_in, n_out, (prp, pci, pv) in ((mx.SPMV_OP_NORMAL, cols, rows, (rp, ci, v)),
+                                                 (mx.SPMV_OP_TRANSPOSE, rows, cols, np_transpose(rp, ci, v, cols))):
+            xh = mx.gen_vector(n_in, 35, dtype=dtype)
+            y_ref, absum = oracle.spmv_ref(prp, pci, pv, xh)
+            y0 = mx.gen_vector(n_out, 36, dtype=dtype)
+            x = cuda.from_numpy(xh).cuda() if n_in else zero
+            y = cuda.from_numpy(y0.copy()).cuda() if n_out else zero.clone()
+            plan.exec_op(op, x, y, -1.5, 0.25)
+            cuda.cuda.synchronize()
+            got = y.cpu().numpy()[:n_out].astype(np.float64)
+            want = -1.5 * y_ref + 0.25 * y0.astype(np.float64)
+            bound = tol_for(dtype) * (1.5 * absum + abs(0.25 * y0.astype(np.float64)))
+            assert (np.abs(got - want) <= bound + (0 if dtype == np.float64 else 1e-30)).all(), (name, fmt, op)
+
+
+def test_convert_refuses_other_formats(mx, cuda, mats):
+    rp, ci, v, cols = mats["poisson"]
+    h = mx.spmv_create_handle()
+    A = device_csr(mx, rp, ci, v, cols)
+    for f in (mx.SPMV_FORMAT_COO, mx.SPMV_FORMAT_BSR, mx.SPMV_FORMAT_CSR2):
+        with pytest.raises(mx.SpmvError) as e:
+            mx.Plan.from_format(h, A, f)
+        assert e.value.status == -7
