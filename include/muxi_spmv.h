@@ -10,7 +10,8 @@
  *
  * Reference interfaces replaced (paths inside the muxi_spmv project):
  *   src/utils/common.h:31-94          status / format / type / op enums, opts
- *   src/api/spmv_api.h:18-92          handle, spmv_exec, spmv_csr_exec
+ *   src/api/spmv_api.h:18-92          handle, spmv_exec (spmv_convert +
+ *                                      spmv_exec_* here), spmv_csr_exec
  *   src/spmv/csr/spmv_csr.cu:52-249   spmv_csr<T> dispatcher
  *   src/spmv/csr5/spmv_csr5.cu:223-362  csr5_preprocess<T>, spmv_csr5<T>
  *   src/spmv/csr5/spmv_csr5.cu:497-533,912-1014  merge-path search,
@@ -22,6 +23,7 @@
  *   src/generators/matrix_generator.h:19-102  synthetic matrix generators
  *   src/generators/mtx_io.h:22-85     Matrix Market reader / writer
  *   src/formats/sparse_formats.h:113-162  COOMatrix (declared there, no kernel)
+ *   src/formats/sparse_formats.h:207-269  BSRMatrix (declared there, no kernel)
  *   src/spmv/csr/spmv_csr.cuh:105-107, src/api/spmv_api.h:70-78  transpose SpMV
  *   tests/test_pinned_memory.cu:245-380  host-memory SpMV (pipelines here)
  *   tests/test_multi_stream.cu:121-236   multi-stream SpMV (batches here)
