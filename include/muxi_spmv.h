@@ -699,9 +699,10 @@ typedef enum {
 SPMV_API spmv_status_t spmv_select(spmv_handle_t* handle, spmv_select_mode_t mode, spmv_mlp_t model, int topK,
                                    spmv_type_t type, int numRows, int numCols, int nnz, const int* rowPtr,
                                    const int* colIdx, const void* values, spmv_variant_t* out, int* spaceIndex);
-/* Registers (model != NULL) or clears a selector model on the handle: plans
- * created with SPMV_KERNEL_AUTO then take the learned pick.  The handle
- * borrows the model; it must outlive the handle's use of it. */
+/* Registers (model != NULL) or clears a selector model on the handle: FP32
+ * plans created with SPMV_KERNEL_AUTO then take the learned pick (the model
+ * is trained on FP32 timings; FP64 AUTO plans keep the FP64 default).  The
+ * handle borrows the model; it must outlive the handle's use of it. */
 SPMV_API spmv_status_t spmv_set_selector(spmv_handle_t* handle, spmv_mlp_t model);
 /* How AUTO plans on this handle use the registered model:
  * SPMV_SELECT_LEARNED (default: the model's pick, about 0.15 ms) or

@@ -11,7 +11,7 @@
 namespace mxs {
 
 spmv_variant_t auto_variant(spmv_type_t type, int nnz) {
-    // Without a selector model: CSR5 tiles with gathers in nonzero order,
+    // Without a selector model (FP64: always): CSR5 tiles with gathers in nonzero order,
     // 128-thread blocks (nnz-balanced, warp-local, the fastest measured
     // variant on irregular matrices) -- 512-nonzero tiles for FP32 (256 when
     // the matrix has empty rows, plan_variant), 256 for FP64; merge-path
@@ -124,7 +124,8 @@ spmv_status_t plan_variant(spmv_handle_t* h, spmv_type_t type, int R, int C, int
     *out = resolve(variant, type, R, N);
     const HandleState* hs = static_cast<const HandleState*>(h->internal);
     const bool autoPick = !variant || variant->kernel == SPMV_KERNEL_AUTO;
-    if (autoPick && !(hs && hs->selector) && out->kernel == SPMV_KERNEL_CSR5 && out->itemsPerThread == 16 && R > 0) {
+    if (autoPick && !(hs && hs->selector && type == SPMV_TYPE_FLOAT) && out->kernel == SPMV_KERNEL_CSR5 &&
+        out->itemsPerThread == 16 && R > 0) {
         // 512-nonzero tiles pay with plan-time row-start masks, which need a
         // matrix without empty rows; otherwise the tile's row search reads
         // rowPtr slices that 512-nonzero tiles overflow: take 256.
@@ -132,14 +133,18 @@ spmv_status_t plan_variant(spmv_handle_t* h, spmv_type_t type, int R, int C, int
         MXS_TRY(count_empty_rows(rowPtr, R, &empties, h->stream));
         if (empties > 0) out->itemsPerThread = 8;
     }
-    if (autoPick && hs && hs->selector && R > 0 && N > 0 && hs->selectorMode == SPMV_SELECT_LEARNED_FALLBACK) {
+    // The model is trained on FP32 timings; FP64 AUTO plans keep the FP64
+    // default (one FMA per nonzero), which beat the model's FP32 picks on
+    // FP64 matrices by 15-28%.
+    const bool useModel = hs && hs->selector && type == SPMV_TYPE_FLOAT;
+    if (autoPick && useModel && R > 0 && N > 0 && hs->selectorMode == SPMV_SELECT_LEARNED_FALLBACK) {
         spmv_variant_t pick{};
         MXS_TRY(spmv_select(h, SPMV_SELECT_LEARNED_FALLBACK, hs->selector, 0, type, R, C, N, rowPtr, colIdx, values,
                             &pick, nullptr));
         *out = resolve(&pick, type, R, N);
         return SPMV_SUCCESS;
     }
-    if (autoPick && hs && hs->selector && R > 0 && N > 0) {
+    if (autoPick && useModel && R > 0 && N > 0) {
         std::vector<int> order;
         MXS_TRY(learned_rank(hs->selector, type, R, C, N, rowPtr, colIdx, h->stream, order));
         std::vector<spmv_variant_t> space(spmv_variant_space(nullptr, 0));

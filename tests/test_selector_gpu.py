@@ -13,7 +13,7 @@ import pytest
 
 import mlp_ref
 import oracle
-from conftest import tol_for
+from conftest import device_csr, tol_for
 
 pytestmark = pytest.mark.gpu
 
@@ -367,6 +367,12 @@ def test_auto_plan_with_registered_selector(mx, sel, cuda):
     assert oracle.row_errors(host(y2), y_ref, absum, tol_for(np.float32)).max() <= 1.0
     with pytest.raises(mx.SpmvError):  # AUTO plans take the learned modes only
         mx.check(mx.lib().spmv_set_selector_mode(h.raw, sel.SELECT_AUTOTUNE), "spmv_set_selector_mode")
+    # FP64 AUTO plans keep the FP64 default whatever the model says (its labels are FP32 timings)
+    A64 = device_csr(mx, rp, ci, v.astype(np.float64), A.numCols)
+    for mode in (sel.SELECT_LEARNED, sel.SELECT_LEARNED_FALLBACK):
+        sel.set_selector(h, model, mode)
+        pv64 = mx.Plan(h, A64).variant
+        assert (pv64.kernel, pv64.blockSize, pv64.itemsPerThread, pv64.vectorWidth) == (mx.KERNEL_CSR5, 128, 8, 32)
     sel.set_selector(h, None)
     assert mx.Plan(h, A).variant.kernel == mx.KERNEL_CSR5
     h.destroy()
