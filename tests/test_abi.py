@@ -90,6 +90,16 @@ def test_argument_errors_without_device(mx):
     o.operation = 1  # transpose: argument checks come before any device work
     st = L.spmv_csr_f32(4, 4, 3, None, None, None, None, None, 1.0, 0.0, C.byref(o))
     assert st == -2 and "rowPtr" in mx.last_error()
+    # the format-generic pair: formats without a plan, missing handle / plan
+    p = C.c_void_p()
+    for fmt in (mx.SPMV_FORMAT_COO, mx.SPMV_FORMAT_CSR2, mx.SPMV_FORMAT_BSR, -1):
+        st = L.spmv_convert(None, mx.SPMV_TYPE_FLOAT, 4, 4, 0, None, None, None, fmt, None, C.byref(p))
+        assert st == -7 and "CSR, CSR5 or ELL" in mx.last_error()
+    for fmt in (mx.SPMV_FORMAT_CSR, mx.SPMV_FORMAT_CSR5, mx.SPMV_FORMAT_ELL):
+        st = L.spmv_convert(None, mx.SPMV_TYPE_FLOAT, 4, 4, 0, None, None, None, fmt, None, C.byref(p))
+        assert st == -1 and not p.value
+    assert L.spmv_exec_f32(None, None, mx.SPMV_OP_NORMAL, 1.0, None, 0.0, None) == -1
+    assert L.spmv_exec_f64(None, None, mx.SPMV_OP_TRANSPOSE, 1.0, None, 0.0, None) == -1
 
 
 def test_reference_partition_count(mx):
