@@ -58,11 +58,16 @@ csr5_tile_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int
 // rFirst plus the set bits up to its first position (a popcount prefix over
 // the words); a set bit inside the lane closes the current row.  Same
 // results as csr5_tile_rows, without reading rowPtr.
+// sY (nullptr: each lane stores its rows into y): a warp region of at least
+// 32*E values.  The rows a tile completes are consecutive from rFirst (one
+// per row start inside the tile, plus the last row when it ends at the tile
+// end); their sums are staged at sY[r - rFirst] and stored to y by one
+// coalesced pass instead of one scattered store per row.
 template <typename T, int E, typename Acc>
 __device__ __forceinline__ void csr5_tile_rows_bits(Acc acc, unsigned word, int rFirst, long long t, int lane,
                                                     int nnz, T* __restrict__ y, T alpha, T beta, bool bz,
                                                     int* __restrict__ carryRow, T* __restrict__ carryVal,
-                                                    bool plain) {
+                                                    bool plain, T* sY) {
     constexpr int SIGMA = 32 * E;
     const int tStart = (int)t * SIGMA;
     const int tEnd = min(tStart + SIGMA, nnz);
@@ -84,6 +89,10 @@ __device__ __forceinline__ void csr5_tile_rows_bits(Acc acc, unsigned word, int 
     const unsigned myBits = (wordW >> o) & (E >= 32 ? 0xffffffffu : ((1u << E) - 1u));
     const unsigned nextFirst = __shfl_down_sync(kFull, myBits & 1u, 1);
 
+    auto put = [&](int r, T s) {
+        if (sY) sY[r - rFirst] = s;
+        else y[r] = axpbyp(plain, alpha, s, beta, bz, y + r);
+    };
     const int j0 = tStart + lane * E;
     const int laneEnd = min(j0 + E, tEnd);
     const bool has = j0 < tEnd;
@@ -99,7 +108,7 @@ __device__ __forceinline__ void csr5_tile_rows_bits(Acc acc, unsigned word, int 
                         headRow = key;
                         headVal = run;
                     } else {
-                        y[key] = axpbyp(plain, alpha, run, beta, bz, y + key);
+                        put(key, run);
                     }
                     ++key;
                     run = T(0);
@@ -123,13 +132,20 @@ __device__ __forceinline__ void csr5_tile_rows_bits(Acc acc, unsigned word, int 
     }
     const int prevKey = __shfl_up_sync(kFull, key, 1);
     const T prevIncl = __shfl_up_sync(kFull, incl2, 1);
-    if (!has) return;
-    const T cin = (lane > 0 && prevKey == startRow) ? prevIncl : T(0);
-    if (headRow >= 0) y[headRow] = axpbyp(plain, alpha, headVal + cin, beta, bz, y + headRow);
-    if (endsHere) y[key] = axpbyp(plain, alpha, incl2, beta, bz, y + key);
-    if (laneEnd == tEnd) {  // the lane holding the tile's last nonzero
-        carryRow[t] = endsHere ? -1 : key;
-        carryVal[t] = incl2;
+    if (has) {
+        const T cin = (lane > 0 && prevKey == startRow) ? prevIncl : T(0);
+        if (headRow >= 0) put(headRow, headVal + cin);
+        if (endsHere) put(key, incl2);
+        if (laneEnd == tEnd) {  // the lane holding the tile's last nonzero
+            carryRow[t] = endsHere ? -1 : key;
+            carryVal[t] = incl2;
+        }
+    }
+    if (sY) {
+        // row starts at positions 1..SIGMA-1 (lane E-1 holds the sum over the words)
+        const int n = __shfl_sync(kFull, incl, E - 1) + (endsAtTileEnd ? 1 : 0);
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) y[rFirst + i] = axpbyp(plain, alpha, sY[i], beta, bz, y + rFirst + i);
     }
 }
 
@@ -225,7 +241,9 @@ __device__ __forceinline__ void csr5_ordered_load(OrderedLoad<T, E>& L, long lon
     L.rLast = t + 1 < tiles ? __ldg(tileRow + t + 1) : numRows - 1;
 }
 
-// Hands this lane's E consecutive terms to the row logic `rows(acc)`.  FP32:
+// Hands this lane's E consecutive terms to the row logic `rows(acc, sY)`;
+// sY is the region once free for staging row sums (FP32) or nullptr (FP64,
+// whose terms still read it).  FP32:
 // the products go through shared memory (one round trip).  FP64: the values,
 // then the gathered x, go through the same region and each term is one FMA
 // -- on GB300 the FP64 pipe, not memory, bounds an FP64 SpMV, and a product
@@ -243,7 +261,7 @@ __device__ __forceinline__ void ordered_handoff(const T (&v)[E], const T (&g)[E]
 #pragma unroll
         for (int e = 0; e < E; ++e) sP[ordered_slot<T, E>(lane + 32 * e)] = g[e];
         __syncwarp();
-        rows([&](T r, int e) { return fma(a[e], sP[ordered_slot<T, E>(lane * E + e)], r); });
+        rows([&](T r, int e) { return fma(a[e], sP[ordered_slot<T, E>(lane * E + e)], r); }, nullptr);
     } else {
 #pragma unroll
         for (int e = 0; e < E; ++e) sP[ordered_slot<T, E>(lane + 32 * e)] = v[e] * g[e];
@@ -251,7 +269,8 @@ __device__ __forceinline__ void ordered_handoff(const T (&v)[E], const T (&g)[E]
         T p[E];
 #pragma unroll
         for (int e = 0; e < E; ++e) p[e] = sP[ordered_slot<T, E>(lane * E + e)];
-        rows([&](T r, int e) { return r + p[e]; });
+        __syncwarp();  // the region is free again: the row logic may stage row sums in it
+        rows([&](T r, int e) { return r + p[e]; }, sP);
     }
 }
 
@@ -286,9 +305,9 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
     }
 
     if (useBits) {
-        ordered_handoff<T, E>(L.v, g, lane, sP, [&](auto acc) {
+        ordered_handoff<T, E>(L.v, g, lane, sP, [&](auto acc, T* sY) {
             csr5_tile_rows_bits<T, E>(acc, L.bits, rFirst, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal,
-                                      plain);
+                                      plain, sY);
         });
         if (REUSE) __syncwarp();
         return;
@@ -302,7 +321,7 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
             if (i < nRp) sRp[i] = __ldg(rowPtr + rFirst + i);
         }
     }
-    ordered_handoff<T, E>(L.v, g, lane, sP, [&](auto acc) {
+    ordered_handoff<T, E>(L.v, g, lane, sP, [&](auto acc, T*) {
         csr5_tile_rows<T, E>(acc, rFirst, rLast, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal,
                              [&](int r) { return (staged && r >= rFirst) ? sRp[r - rFirst] : __ldg(rowPtr + r); },
                              noEmpty, plain);
