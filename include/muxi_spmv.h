@@ -461,7 +461,9 @@ SPMV_API spmv_status_t spmv_plan_exec_f64(spmv_handle_t* handle, spmv_plan_t pla
 /* y = alpha*op(A)*x + beta*y with op = SPMV_OP_NORMAL (as spmv_plan_exec_*)
  * or SPMV_OP_TRANSPOSE (x: numRows entries, y: numCols).  The transpose is
  * built from the matrix's values on the first transposed call and kept with
- * the plan (a caller that changes the values recreates the plan).
+ * the plan (a caller that changes the values recreates the plan).  That first
+ * call allocates and synchronises the handle's stream: make it before
+ * capturing transposed executions into a CUDA graph.
  * SPMV_OP_CONJUGATE: SPMV_ERROR_UNSUPPORTED_FORMAT. */
 SPMV_API spmv_status_t spmv_plan_exec_op_f32(spmv_handle_t* handle, spmv_plan_t plan, spmv_operation_t op,
                                              float alpha, const float* x, float beta, float* y);
