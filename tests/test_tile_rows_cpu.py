@@ -50,3 +50,44 @@ def test_completed_rows_are_consecutive_from_first_row(name, sigma):
         n = len(starts[t]) + int(ends_at_end[t])
         assert np.array_equal(completed, np.arange(tile_row[t], tile_row[t] + n)), (name, sigma, t)
         assert n <= sigma  # the staging region holds at least 32*E = sigma values
+
+
+def kogge_stone_segmented(keys, vals, max_steps=None):
+    """The warp scan of the tile row logic, lane by lane: step `off` adds the
+    value of lane - off when that lane has the same key."""
+    v = np.array(vals, dtype=np.float64)
+    off, steps = 1, 0
+    while off < 32 and (max_steps is None or steps < max_steps):
+        prev = v.copy()
+        for lane in range(off, 32):
+            if keys[lane - off] == keys[lane]:
+                v[lane] = prev[lane] + prev[lane - off]
+        off <<= 1
+        steps += 1
+    return v
+
+
+def test_segmented_scan_stops_at_longest_key_run():
+    """key_run_length: with keys rising over the lanes, the steps whose offset
+    is below the longest run of equal keys already give the full scan (the
+    FP64 tiles skip the rest)."""
+    rng = np.random.default_rng(3)
+    for _ in range(2000):
+        run_cap = int(rng.integers(1, 33))
+        lens = []
+        while sum(lens) < 32:
+            lens.append(int(rng.integers(1, run_cap + 1)))
+        keys = np.repeat(np.arange(len(lens)), lens)[:32]
+        if rng.random() < 0.2:  # lanes without elements carry the largest key at the end
+            keys[32 - int(rng.integers(1, 16)):] = 0x7FFFFFFF
+        vals = rng.integers(-1000, 1000, 32).astype(np.float64)  # exact sums
+        span = max(int(np.sum(keys[: l + 1] == keys[l])) for l in range(32))
+        steps = 0
+        while (1 << steps) < span:
+            steps += 1
+        full = kogge_stone_segmented(keys, vals)
+        short = kogge_stone_segmented(keys, vals, max_steps=steps)
+        assert np.array_equal(full, short), (keys, span)
+        # and the full scan is the segmented inclusive prefix sum
+        ref = np.array([vals[: l + 1][keys[: l + 1] == keys[l]].sum() for l in range(32)])
+        assert np.array_equal(full, ref)
