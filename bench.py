@@ -409,7 +409,7 @@ def gpu_arm(args):
     pv = plan.variant.as_dict()
     kern_names = {mx.KERNEL_MERGE: "merge_vec_kernel",
                   mx.KERNEL_CSR5: "csr5_ordered_kernel" if pv["vectorWidth"] == 32 else "csr5_tile_kernel",
-                  mx.KERNEL_BAND: "band_block_kernel", mx.KERNEL_ELL: "ell_kernel",
+                  mx.KERNEL_BAND: "csr5_window_kernel", mx.KERNEL_ELL: "ell_kernel",
                   mx.KERNEL_SCALAR: "csr_rows_kernel", mx.KERNEL_VECTOR: "csr_rows_kernel"}
     # merge-path, CSR5 and band plans launch the tile kernel and a carry fix-up
     launches_per_step = 2 if pv["kernel"] in (mx.KERNEL_MERGE, mx.KERNEL_CSR5, mx.KERNEL_BAND) else 1

@@ -255,9 +255,10 @@ typedef enum {
     SPMV_KERNEL_CSR5 = 4,      /* sigma-nnz tiles (CSR5 metadata)           */
     SPMV_KERNEL_ELL = 5,       /* column-major ELLPACK                      */
     SPMV_KERNEL_HEURISTIC = 6, /* plan: the reference's avgNnz rule, restated */
-    SPMV_KERNEL_BAND = 7       /* CSR5 tiles of 32*itemsPerThread nonzeros in persistent
-                                  CTAs of blockSize threads that keep a sliding shared-
-                                  memory window of x around the diagonal             */
+    SPMV_KERNEL_BAND = 7       /* ordered CSR5 tiles of 32*itemsPerThread nonzeros; each
+                                  CTA owns a range of consecutive tiles and serves the
+                                  gathers that fall in a bulk-copied shared-memory
+                                  window of x around its rows from there            */
 } spmv_kernel_t;
 
 /* One launch configuration of a kernel family. */
@@ -265,17 +266,26 @@ typedef struct {
     spmv_kernel_t kernel;
     int blockSize;       /* threads per CTA: SCALAR/VECTOR 64..1024 (powers
                             of two), MERGE 128/256, CSR5 with vectorWidth
-                            32 128..1024, others 256 or 512               */
+                            32 128..1024, BAND 256/512/1024 (0: 512),
+                            others 256 or 512                             */
     int threadsPerRow;   /* VECTOR: 1,2,4,8,16,32; CSR5 with vectorWidth 32:
                             0 = one tile per warp; n > 0 = block ranges:
-                            a block of blockSize 256/512/1024 threads owns
-                            n tiles per warp of consecutive tiles, which
-                            its warps take one at a time                  */
+                            a block of blockSize 256/384/512/640/1024
+                            threads owns about n tiles per warp of
+                            consecutive tiles (fitted so the blocks fill
+                            whole waves; n beyond the tiles per resident
+                            block gives each resident block one range),
+                            which its warps take one at a time; BAND: target
+                            tiles per warp of a CTA's range (0: 8), fitted
+                            so the CTAs fill whole waves                  */
     int itemsPerThread;  /* MERGE: merge items per thread (tile = block*ipt);
-                            CSR5/BAND: nonzeros per lane (tile = 32*ipt)   */
+                            CSR5: nonzeros per lane (tile = 32*ipt);
+                            BAND: 8 or 16 (0: 16 for FP32, 8 for FP64)   */
     int vectorWidth;     /* VECTOR/MERGE: 1 or 4 elements per load;
                             CSR5: 32 = gathers issued in nonzero order
-                            (32 consecutive nonzeros per instruction)      */
+                            (32 consecutive nonzeros per instruction);
+                            BAND: x window in units of 1,024 elements
+                            (0: the largest the CTA shape fits)           */
 } spmv_variant_t;
 
 /* Run one explicit variant (no plan, no selector).  MERGE variants take
@@ -489,11 +499,22 @@ SPMV_API spmv_status_t spmv_exec_f32(spmv_handle_t* handle, spmv_plan_t plan, sp
 SPMV_API spmv_status_t spmv_exec_f64(spmv_handle_t* handle, spmv_plan_t plan, spmv_operation_t op, double alpha,
                                      const double* x, double beta, double* y);
 
-/* Device-side failure word of a plan.  The pipelined BAND kernel never waits
- * without a bound: a wait that gives up (about 2 s) raises this word and the
- * kernel returns.  Synchronises; *code = 0 when clean, else the raised code
- * (the call then returns SPMV_ERROR_DEVICE and clears the word). */
+/* Device-side failure word of a plan.  The BAND kernel's wait for its
+ * bulk-copied x window is bounded: a wait that gives up (about 2 s) raises
+ * this word (code 2), lets the copy land and returns without computing.
+ * Synchronises; *code = 0 when clean, else the raised code (the call then
+ * returns SPMV_ERROR_DEVICE and clears the word). */
 SPMV_API spmv_status_t spmv_plan_device_error(spmv_plan_t plan, int* code);
+
+/* Fault injection for tests (no reference counterpart; the reference has no
+ * bounded waits).  enable != 0: the following executions of a BAND plan
+ * initialise the window barrier with one arrival held back and wait for it at
+ * most `limitCycles` SM clocks (0: 100,000), so every wait runs out; the
+ * kernel then makes the held-back arrival itself, waits for its copy to land
+ * and returns, and spmv_plan_device_error reports code 2.  The GPU context
+ * stays usable.  enable = 0 restores normal executions.  Plans of other
+ * kernels have no waits: SPMV_ERROR_UNSUPPORTED_FORMAT. */
+SPMV_API spmv_status_t spmv_plan_inject_wait_timeout(spmv_plan_t plan, int enable, long long limitCycles);
 
 /* Kernel timing on the launching stream (the role of the reference's
  * GpuTimer, src/utils/timer.h:17-47, moved into the plan): while enabled,

@@ -366,11 +366,17 @@ class Plan:
         return y
 
     def device_error(self) -> int:
-        """Device failure word of the plan's pipelined kernel (0 = clean);
-        raises SpmvError when it is set."""
+        """Device failure word of the plan (0 = clean): raised when the BAND
+        kernel's bounded window wait gave up; raises SpmvError when set."""
         code = C.c_int()
         check(lib().spmv_plan_device_error(self._p, C.byref(code)), "spmv_plan_device_error")
         return code.value
+
+    def inject_wait_timeout(self, enable: bool = True, limit_cycles: int = 0):
+        """Tests: make the BAND kernel's window wait run out (see
+        spmv_plan_inject_wait_timeout)."""
+        check(lib().spmv_plan_inject_wait_timeout(self._p, 1 if enable else 0, int(limit_cycles)),
+              "spmv_plan_inject_wait_timeout")
 
     def profile(self, enable: bool = True):
         """Records CUDA events around the main kernel of every exec."""

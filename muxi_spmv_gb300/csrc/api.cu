@@ -51,6 +51,7 @@ const DeviceProps& device_props(int dev) {
             p.sm_count = prop.multiProcessorCount;
             p.l2_bytes = prop.l2CacheSize;
             p.smem_optin = prop.sharedMemPerBlockOptin;
+            p.smem_per_sm = prop.sharedMemPerMultiprocessor;
             p.cc_major = prop.major;
             p.cc_minor = prop.minor;
         }

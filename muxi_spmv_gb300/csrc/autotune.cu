@@ -38,9 +38,9 @@ static const spmv_variant_t kSpace[] = {
     {SPMV_KERNEL_CSR5, 256, 0, 8, 32},
     {SPMV_KERNEL_CSR5, 128, 0, 16, 32},
     {SPMV_KERNEL_CSR5, 512, 0, 8, 32},
-    {SPMV_KERNEL_BAND, 256, 0, 4, 4},
-    {SPMV_KERNEL_BAND, 256, 0, 8, 4},
-    {SPMV_KERNEL_BAND, 512, 0, 8, 4},
+    {SPMV_KERNEL_BAND, 512, 0, 16, 0},
+    {SPMV_KERNEL_BAND, 512, 0, 8, 0},
+    {SPMV_KERNEL_BAND, 1024, 0, 16, 0},
     {SPMV_KERNEL_ELL, 256, 0, 0, 1},
 };
 constexpr int kSpaceSize = (int)(sizeof(kSpace) / sizeof(kSpace[0]));

@@ -1,143 +1,244 @@
-// CSR5-tile SpMV with a shared-memory window of x per CTA (the BAND kernel).
+// Ordered CSR5 tiles with a shared-memory window of x per CTA (the BAND
+// kernel family).
 //
-// A CTA of NW warps takes NW*TPW consecutive CSR5 tiles (SIGMA = 32*E
-// nonzeros each); warp w walks TPW consecutive tiles of that block.  Before
-// the gathers, the CTA copies the slice of x around its rows into shared
-// memory with one bulk copy (cp.async.bulk completing on an mbarrier):
-// for rows [R0, R1] the window is [R0 - b, R1 + b] with b chosen so the slice
-// fills WCAP entries.  Gathers whose column lies in the window read shared
-// memory; all others read x from global memory, so results never depend on
-// the window -- only speed.  Banded and diagonally dominant matrices (the
-// stencils, the near-diagonal 70% of the power-law workload) turn most
-// gathers into shared-memory reads, relieving the L1 data pipe that random
-// global gathers saturate, while the window stays small enough for about
-// 48 warps per SM.
+// CSR5 tiles (reference: spmv_csr5_warp32_kernel,
+// src/spmv/csr5/spmv_csr5.cu:148-219) are processed exactly as the ordered
+// kernels do (csr5_ordered.cuh: loads and gathers in nonzero order, interior
+// tiles as warp sums, row logic for the rest, carries fixed up in tile order),
+// but each CTA owns a block range of consecutive tiles and first copies the
+// slice of x around its rows into shared memory with one bulk copy
+// (cp.async.bulk completing on an mbarrier).  A gather whose column lies in
+// the window reads shared memory; every other gather reads x from global
+// memory, so the window changes only speed, never results.
 //
-// The tile data of a warp's first tile is requested before the window wait.
-// The wait gives up after about two seconds: the CTA raises *errFlag and
-// returns (its copy, if still in flight, completes into the CTA's own shared
-// memory first because every thread waits on the same barrier).
+// Why: on matrices whose columns cluster near the diagonal (the 70% near
+// share of the power-law workload, stencils, banded matrices), the gathers of
+// one tile touch a few hundred distinct x sectors that neighbouring tiles on
+// other SMs touch again.  Each such gather is an L1 miss request to L2, and
+// that request path is the busiest unit of the one-tile-per-warp kernel.  The
+// window turns those gathers into shared-memory reads: the x slice crosses
+// from L2 once per CTA (one bulk copy of W elements for perBlock * sigma
+// nonzeros), and only the far gathers still go to L2.
+//
+// Window placement: the CTA's rows [R0, R1] map to columns by the aspect
+// ratio C/R; the window of `winCap` elements is centred there and clamped to
+// [0, C), with its start a multiple of 16 bytes.  When x is not 16-byte
+// aligned the host passes winCap = 0 and every gather reads global memory
+// (the dynamic shared memory is then one 16-byte unit).
+//
+// Waits: each thread waits once on the window's mbarrier, with an iteration
+// limit.  A thread that gives up raises *errFlag (code 2), then waits again,
+// bounded, so that the copy into its CTA's shared memory has landed before the
+// CTA can leave, and returns without computing.  The host reads the flag with
+// spmv_plan_device_error.  For tests, `inject` initialises the barrier with
+// one arrival that nobody makes until a thread has given up (so the first wait
+// always runs out) and `waitLimit` shortens that wait; thread 0 then makes the
+// missing arrival, which lets every thread's draining wait complete.
 #include "internal.h"
 #include "device.cuh"
 #include "kernels.h"
 #include "formats.h"
-#include "csr5_tile.cuh"
+#include "csr5_ordered.cuh"
 
 namespace mxs {
 
-template <typename T, int NW, int E, int TPW, int WCAP>
-__global__ void __launch_bounds__(NW * 32)
-band_block_kernel(int numRows, int numCols, int nnz, const int* __restrict__ rowPtr, const int* __restrict__ colIdx,
-                  const T* __restrict__ values, const T* __restrict__ x, T* __restrict__ y, T alpha, T beta,
-                  int betaZero, const int* __restrict__ tileRow, long long tiles, int useWindow,
-                  int* __restrict__ carryRow, T* __restrict__ carryVal, int* __restrict__ errFlag) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    T* win = reinterpret_cast<T*>(smem);
-    __shared__ int sRpAll[NW][csr5_rp_cap<E>()];
-    __shared__ __align__(8) unsigned long long bar;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const bool bz = betaZero != 0;
-
-    const long long tb = (long long)blockIdx.x * NW * TPW;
-    const long long te = tb + NW * TPW < tiles ? tb + NW * TPW : tiles;
-
-    // Window bounds (uniform per CTA), multiples of 4 elements.
-    int wlo = 0, wspan = 0;
-    if (useWindow) {
-        const int R0 = __ldg(tileRow + tb);
-        const int R1 = te < tiles ? __ldg(tileRow + te) : numRows - 1;
-        const long long rows = (long long)R1 - R0 + 1;
-        const long long b = rows < WCAP ? (WCAP - rows) / 2 : 0;
-        long long lo = (long long)R0 - b;
-        lo = lo < 0 ? 0 : lo & ~3LL;
-        long long hi = lo + WCAP;
-        const long long cols4 = numCols & ~3LL;
-        if (hi > cols4) hi = cols4;
-        if (hi < lo) hi = lo;
-        wlo = (int)lo;
-        wspan = (int)(hi - lo);
+// Gather through the CTA's window: columns in [lo, lo + span) from shared
+// memory, all others from global memory.  One generic load per gather: the
+// lane picks the address (window slot or x + c) and the load unit routes
+// shared-window addresses to shared memory and the rest to global memory, so
+// a lane's E gathers stay independent loads in flight together, each with
+// one destination register.
+template <typename T>
+struct WindowGather {
+    const T* __restrict__ x;
+    const T* win;  // generic address of the window
+    int lo, span;
+    __device__ __forceinline__ T operator()(int c) const {
+        const unsigned o = (unsigned)(c - lo);
+        const T* p = o < (unsigned)span ? win + o : x + c;
+        return *p;
     }
-    if (tid == 0 && wspan > 0) {
-        mbar_init(&bar, 1);
-        fence_barrier_init();
+};
+
+// Window [lo, lo + span) for rows [R0, R1]: centred on the rows' diagonal
+// position (scaled by C/R), clamped to the 16-byte units of x, start a
+// multiple of 16 bytes.  span = 0 when no window is used.
+template <typename T>
+__device__ __forceinline__ void window_bounds(int R0, int R1, int numRows, int numCols, int cap, int& lo,
+                                              int& span) {
+    constexpr long long A = 16 / sizeof(T);  // elements per 16-byte unit
+    const long long cols = (long long)numCols / A * A;
+    lo = 0;
+    span = 0;
+    if (cap <= 0 || cols <= 0) return;
+    long long mid = ((long long)R0 + R1) / 2;
+    if (numRows != numCols && numRows > 0) mid = mid * numCols / numRows;
+    long long l = mid - cap / 2;
+    if (l > cols - cap) l = cols - cap;
+    if (l < 0) l = 0;
+    l = l / A * A;
+    const long long h = l + cap < cols ? l + cap : cols;
+    lo = (int)l;
+    span = (int)(h - l);
+}
+
+// Waits for the window; false when the wait gave up (after draining the copy).
+__device__ __forceinline__ bool window_wait(unsigned long long* bar, long long limit, int inject,
+                                            int* __restrict__ errFlag) {
+    if (mbar_wait_bounded(bar, 0, limit)) return true;
+    atomicExch(errFlag, 2);
+    if (inject && threadIdx.x == 0) mbar_arrive(bar);  // the arrival held back by the test
+    mbar_wait_bounded(bar, 0, kWaitLimitCycles);        // the bulk copy lands before the CTA leaves
+    return false;
+}
+
+// One CTA per block range of `perBlock` tiles; its warps draw the range's
+// tiles one at a time from a shared counter (neighbouring rows in flight
+// together, no block waits on one long tile).  Dynamic shared memory: the
+// window, winCap elements.
+template <typename T, int E, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB)
+csr5_window_kernel(int numRows, int numCols, int nnz, const int* __restrict__ rowPtr,
+                   const int* __restrict__ colIdx, const T* __restrict__ values, const T* __restrict__ x,
+                   T* __restrict__ y, T alpha, T beta, int betaZero, const int* __restrict__ tileRow, long long tiles,
+                   int* __restrict__ carryRow, T* __restrict__ carryVal, int noEmptyRows, int perBlock,
+                   const unsigned* __restrict__ tileBits, int winCap, int* __restrict__ errFlag, long long waitLimit,
+                   int inject) {
+    constexpr int WARPS = BLOCK / 32;
+    extern __shared__ __align__(128) unsigned char smemDyn[];
+    T* win = reinterpret_cast<T*>(smemDyn);
+    __shared__ int sRpAll[WARPS][kOrderedRpCap];
+    __shared__ __align__(16) T sPAll[WARPS][ordered_slots<T, E>()];
+    __shared__ int sNext;
+    __shared__ __align__(8) unsigned long long bar;
+    pdl_trigger();  // the carry fix-up may be scheduled behind the last wave
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // Tile counts fit in int: plans cap nnz below 2^31.
+    const int tb = blockIdx.x * perBlock;
+    const int te = min(tb + perBlock, (int)tiles);
+    int lo, span;
+    window_bounds<T>(__ldg(tileRow + tb), te < tiles ? __ldg(tileRow + te) : numRows - 1, numRows, numCols, winCap,
+                     lo, span);
+    if (threadIdx.x == 0) {
+        sNext = tb + WARPS;
+        if (span > 0) {
+            mbar_init(&bar, inject ? 2 : 1);
+            fence_barrier_init();
+        }
     }
     __syncthreads();
-    if (tid == 0 && wspan > 0) {
-        mbar_arrive_expect_tx(&bar, (unsigned)(wspan * sizeof(T)));
-        bulk_g2s(win, x + wlo, (unsigned)(wspan * sizeof(T)), &bar);
+    if (threadIdx.x == 0 && span > 0) {
+        mbar_arrive_expect_tx(&bar, (unsigned)(span * sizeof(T)));
+        bulk_g2s(win, x + lo, (unsigned)(span * sizeof(T)), &bar);
     }
+    const WindowGather<T> gather{x, win, lo, span};
+    const bool bz = betaZero != 0, plain = betaZero == kPlainAxpby;
+    const bool useBits = tileBits != nullptr, noEmpty = noEmptyRows != 0;
 
-    long long t = tb + (long long)warp * TPW;
-    const long long tw = t + TPW < te ? t + TPW : te;
-    Csr5Load<T, E> cur;
-    if (t < tw) csr5_load<T, E>(cur, t, lane, nnz, tiles, numRows, tileRow, rowPtr, colIdx, values);
-    if (wspan > 0 && !mbar_wait_bounded(&bar, 0)) {
-        if (tid == 0) atomicExch(errFlag, 1);
-        return;
-    }
-    int* sRp = sRpAll[warp];
-    for (; t < tw; ++t) {
-        csr5_compute<T, E>(cur, t, lane, numRows, nnz, rowPtr, y, alpha, beta, bz, carryRow, carryVal, sRp,
-                           [x, win, wlo, wspan](int c) {
-                               const unsigned o = (unsigned)(c - wlo);
-                               return o < (unsigned)wspan ? win[o] : ld_x(x + c);
-                           });
-        __syncwarp();
-        if (t + 1 < tw) csr5_load<T, E>(cur, t + 1, lane, nnz, tiles, numRows, tileRow, rowPtr, colIdx, values);
+    int t = tb + w;
+    OrderedLoad<T, E> L;
+    if (t < te) csr5_ordered_load<T, E>(L, t, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
+    // every thread waits (also warps without a tile: the CTA stays until the copy has landed)
+    if (span > 0 && !window_wait(&bar, waitLimit, inject, errFlag)) return;
+    while (t < te) {
+        int next = 0;  // drawn before the compute so its latency hides under the gathers
+        if (lane == 0) next = atomicAdd(&sNext, 1);
+        csr5_ordered_compute<T, E, true>(L, t, lane, nnz, rowPtr, gather, y, alpha, beta, bz, tiles, carryRow,
+                                         carryVal, noEmpty, sRpAll[w], sPAll[w], useBits, plain);
+        t = __shfl_sync(kFull, next, 0);
+        if (t < te) csr5_ordered_load<T, E>(L, t, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
     }
 }
-
-template <typename T> constexpr int block_window_cap() { return sizeof(T) == 4 ? 8192 : 4096; }
 
 bool band_shape_supported(int block, int E) {
-    return (block == 256 || block == 512) && (E == 4 || E == 8);
+    return (block == 256 || block == 512 || block == 1024) && (E == 8 || E == 16);
 }
 
-template <typename T, int NW, int E>
-static spmv_status_t launch_block(const int* tileRow, long long tiles, int* carryRow, T* carryVal, int* errFlag,
-                                  const RowsArgs<T>& a, int numCols, cudaStream_t s) {
-    constexpr int TPW = 4;
-    constexpr int WCAP = block_window_cap<T>();
-    const bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0;
-    const size_t smem = aligned ? sizeof(T) * WCAP : 0;
-    auto kern = band_block_kernel<T, NW, E, TPW, WCAP>;
-    static bool attr[64] = {false};
+// Default window capacity (elements) of a shape: the largest multiple of
+// 1,024 elements that keeps MINB CTAs per SM within the SM's shared memory
+// (228 KB, 1 KB of it reserved per CTA), capped at 32,768.
+template <typename T, int E, int BLOCK, int MINB>
+static int default_window(const DeviceProps& dp) {
+    constexpr size_t staticBytes = (BLOCK / 32) * (kOrderedRpCap * sizeof(int) + ordered_slots<T, E>() * sizeof(T)) + 64;
+    const size_t smPerSm = dp.smem_per_sm ? dp.smem_per_sm : 233472;
+    const size_t perCta = smPerSm / MINB - 1024;
+    size_t room = perCta > staticBytes ? perCta - staticBytes : 0;
+    if (dp.smem_optin && room + staticBytes > dp.smem_optin) room = dp.smem_optin - staticBytes;
+    long long elems = (long long)(room / sizeof(T)) / 1024 * 1024;
+    if (elems > 32768) elems = 32768;
+    return (int)(elems < 0 ? 0 : elems);
+}
+
+template <typename T, int E, int BLOCK, int MINB>
+static spmv_status_t launch_window(const int* tileRow, long long tiles, int* carryRow, T* carryVal, int* errFlag,
+                                   const RowsArgs<T>& a, int numCols, int tilesPerWarp, int winK,
+                                   const unsigned* bits, const BandTest& test, cudaStream_t s) {
+    auto kern = csr5_window_kernel<T, E, BLOCK, MINB>;
     int dev = 0;
     MXS_CUDA(cudaGetDevice(&dev));
-    if (dev >= 64 || !attr[dev]) {
-        MXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(T) * WCAP)));
-        // Prefer the largest shared-memory carve-out so several CTAs' windows fit per SM.
+    const DeviceProps& dp = device_props(dev);
+    const int maxWin = default_window<T, E, BLOCK, MINB>(dp);
+    int cap = winK > 0 ? winK * 1024 : maxWin;
+    if (cap > maxWin) cap = maxWin;
+    const bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0;
+    if (!aligned) cap = 0;
+    static bool attrSet[64] = {false};
+    if (dev >= 64 || !attrSet[dev]) {
+        MXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(sizeof(T) * (size_t)maxWin > 16 ? sizeof(T) * (size_t)maxWin : 16)));
         MXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-        if (dev < 64) attr[dev] = true;
+        if (dev < 64) attrSet[dev] = true;
     }
-    const long long perCta = (long long)NW * TPW;
-    const long long grid = (tiles + perCta - 1) / perCta;
-    if (grid > 0x7fffffffLL) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "too many tiles");
-    kern<<<(unsigned)grid, NW * 32, smem, s>>>(a.numRows, numCols, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y,
-                                               a.alpha, a.beta, a.betaZero, tileRow, tiles, aligned ? 1 : 0,
-                                               carryRow, carryVal, errFlag);
+    // at least one 16-byte unit, also when no window is used
+    const size_t smem = sizeof(T) * (size_t)cap > 16 ? sizeof(T) * (size_t)cap : 16;
+    // Whole waves: CTAs hold equal nonzero counts, so the range length is
+    // picked to make the CTA count a multiple of the CTAs resident at once.
+    int perSm = 0;
+    MXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, BLOCK, smem));
+    if (perSm < 1) MXS_FAIL(SPMV_ERROR_INTERNAL, "window kernel does not fit an SM (window %d elements)", cap);
+    const long long resident = (long long)perSm * dp.sm_count;
+    const long long per = fitted_range(tiles, (long long)(tilesPerWarp > 0 ? tilesPerWarp : 8) * (BLOCK / 32),
+                                       resident, BLOCK / 32);
+    if (per > 0x7fffffffLL) MXS_FAIL(SPMV_ERROR_INTERNAL, "block range too large");
+    const long long grid = (tiles + per - 1) / per;
+    const int bzFlags = a.betaZero ? (a.alpha == T(1) ? kPlainAxpby : 1) : 0;
+    kern<<<(unsigned)grid, BLOCK, smem, s>>>(a.numRows, numCols, a.nnz, a.rowPtr, a.colIdx, a.values, a.x, a.y,
+                                             a.alpha, a.beta, bzFlags, tileRow, tiles, carryRow, carryVal,
+                                             a.noEmptyRows, (int)per, bits, cap, errFlag,
+                                             test.waitLimit > 0 ? test.waitLimit : kWaitLimitCycles,
+                                             test.inject ? 1 : 0);
     MXS_LAUNCH_CHECK();
     return SPMV_SUCCESS;
 }
 
 template <typename T>
-spmv_status_t run_band(int block, int E, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
-                       int* errFlag, const RowsArgs<T>& a, int numCols, cudaStream_t s, cudaEvent_t afterMain) {
+spmv_status_t run_band(int block, int E, int tilesPerWarp, int winK, const int* tileRow, long long tiles,
+                       int* carryRow, T* carryVal, int* errFlag, const RowsArgs<T>& a, int numCols, cudaStream_t s,
+                       cudaEvent_t afterMain, const Csr5Chains* chains, const unsigned* tileBits,
+                       const BandTest& test) {
     if (tiles <= 0) return SPMV_SUCCESS;
+    constexpr bool wide = sizeof(T) == 8;
     spmv_status_t st;
-    if (block == 512 && E == 8) st = launch_block<T, 16, 8>(tileRow, tiles, carryRow, carryVal, errFlag, a, numCols, s);
-    else if (block == 512 && E == 4) st = launch_block<T, 16, 4>(tileRow, tiles, carryRow, carryVal, errFlag, a, numCols, s);
-    else if (block == 256 && E == 8) st = launch_block<T, 8, 8>(tileRow, tiles, carryRow, carryVal, errFlag, a, numCols, s);
-    else if (block == 256 && E == 4) st = launch_block<T, 8, 4>(tileRow, tiles, carryRow, carryVal, errFlag, a, numCols, s);
+#define MXS_WIN(B, EE, M)                                                                                 \
+    st = launch_window<T, EE, B, M>(tileRow, tiles, carryRow, carryVal, errFlag, a, numCols, tilesPerWarp, \
+                                    winK, tileBits, test, s)
+    if (block == 512 && E == 16) MXS_WIN(512, 16, 2);
+    else if (block == 512 && E == 8) MXS_WIN(512, 8, 2);
+    else if (block == 1024 && E == 16) MXS_WIN(1024, 16, 1);
+    else if (block == 1024 && E == 8) MXS_WIN(1024, 8, wide ? 1 : 2);
+    else if (block == 256 && E == 16) MXS_WIN(256, 16, wide ? 3 : 4);
+    else if (block == 256 && E == 8) MXS_WIN(256, 8, 4);
     else MXS_FAIL(SPMV_ERROR_INTERNAL, "unsupported band shape block=%d ept=%d", block, E);
+#undef MXS_WIN
     MXS_TRY(st);
-    if (afterMain) MXS_CUDA(cudaEventRecord(afterMain, s));
-    return run_csr5_fixup<T>(tiles, carryRow, carryVal, a, s);
+    return run_csr5_fixups<T>(tiles, carryRow, carryVal, a, s, afterMain, chains, true);
 }
 
-template spmv_status_t run_band<float>(int, int, const int*, long long, int*, float*, int*, const RowsArgs<float>&,
-                                       int, cudaStream_t, cudaEvent_t);
-template spmv_status_t run_band<double>(int, int, const int*, long long, int*, double*, int*,
-                                        const RowsArgs<double>&, int, cudaStream_t, cudaEvent_t);
+template spmv_status_t run_band<float>(int, int, int, int, const int*, long long, int*, float*, int*,
+                                       const RowsArgs<float>&, int, cudaStream_t, cudaEvent_t, const Csr5Chains*,
+                                       const unsigned*, const BandTest&);
+template spmv_status_t run_band<double>(int, int, int, int, const int*, long long, int*, double*, int*,
+                                        const RowsArgs<double>&, int, cudaStream_t, cudaEvent_t, const Csr5Chains*,
+                                        const unsigned*, const BandTest&);
 
 }  // namespace mxs

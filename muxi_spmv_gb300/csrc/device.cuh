@@ -184,14 +184,18 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
         : "memory");
     return ok != 0;
 }
+// Default limit of a bounded wait: about two seconds of SM clock.
+constexpr long long kWaitLimitCycles = 4000000000LL;
+
 // Waits for the phase with the given parity to complete; gives up after
-// about two seconds and returns false (the caller records the failure).
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+// `limit` SM clocks and returns false (the caller records the failure).
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  long long limit = kWaitLimitCycles) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long start = clock64();
     for (;;) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (clock64() - start > 4000000000LL) return false;
+        if (clock64() - start > limit) return false;
         __nanosleep(64);
     }
 }

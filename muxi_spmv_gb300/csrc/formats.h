@@ -32,6 +32,32 @@ spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carr
                        int block = 256, int chunk = 0, const Csr5Chains* chains = nullptr,
                        const unsigned* tileBits = nullptr);
 
+// The carry fix-up behind a CSR5-tiled kernel: with a chain table, one
+// thread (or warp) per chain; without one, runs of carryRow walked in tile
+// order.  `programmatic`: the tile kernel triggers a programmatic launch, so
+// the fix-up is scheduled behind its last wave -- unless an event
+// (`afterMain`, recorded here first) sits between them.
+template <typename T>
+spmv_status_t run_csr5_fixups(long long tiles, const int* carryRow, const T* carryVal, const RowsArgs<T>& a,
+                              cudaStream_t s, cudaEvent_t afterMain, const Csr5Chains* chains, bool programmatic);
+
+// Ordered CSR5 tiles over a shared-memory x window per CTA (band_kernels.cu).
+// E = nonzeros per lane (8, 16), block = threads per CTA (256, 512, 1024);
+// tilesPerWarp: target tiles per warp of a CTA's block range (0: 8); winK:
+// window capacity in units of 1,024 elements (0: the largest the shape
+// fits).  tileRow / carries / chains / tileBits as run_csr5.  errFlag: device
+// int raised (code 2) when a window wait gave up.
+struct BandTest {
+    long long waitLimit = 0;  // SM clocks of the window wait (0: the default, about two seconds)
+    bool inject = false;      // hold back one arrival of the window barrier (the wait runs out)
+};
+bool band_shape_supported(int block, int E);
+template <typename T>
+spmv_status_t run_band(int block, int E, int tilesPerWarp, int winK, const int* tileRow, long long tiles,
+                       int* carryRow, T* carryVal, int* errFlag, const RowsArgs<T>& a, int numCols, cudaStream_t s,
+                       cudaEvent_t afterMain, const Csr5Chains* chains, const unsigned* tileBits,
+                       const BandTest& test);
+
 // Row-start masks of a CSR5 tiling for an ordered plan (matrices without
 // empty rows): sigma/32 words per tile, one cudaMalloc'd buffer in *buf.
 spmv_status_t csr5_tile_bits(const int* rowPtr, int numRows, int sigma, long long tiles, void** buf, cudaStream_t s);

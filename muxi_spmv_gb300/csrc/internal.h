@@ -42,6 +42,7 @@ struct DeviceProps {
     int sm_count = 0;
     size_t l2_bytes = 0;
     size_t smem_optin = 0;
+    size_t smem_per_sm = 0;
     int cc_major = 0, cc_minor = 0;
 };
 const DeviceProps& device_props(int dev);

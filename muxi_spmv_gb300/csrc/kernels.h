@@ -74,15 +74,18 @@ spmv_status_t run_merge(const MergeGeom& g, long long P, const MergeScratch& sc,
 template <typename T>
 spmv_status_t run_merge_fixup(long long P, const MergeScratch& sc, const RowsArgs<T>& a, cudaStream_t s);
 
-// Bulk-copy-pipelined CSR5-tile kernel over a shared-memory x window
-// (band_kernels.cu).  E = nonzeros per lane (4, 8), block = consumer threads
-// (128, 256); tileRow holds the CSR5 tile rows for sigma = 32*E; carries as
-// run_csr5.  errFlag: device int raised (non-zero) if a pipeline wait gave up.
-bool band_shape_supported(int block, int E);
-template <typename T>
-spmv_status_t run_band(int block, int E, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
-                       int* errFlag, const RowsArgs<T>& a, int numCols, cudaStream_t s,
-                       cudaEvent_t afterMain = nullptr);
+// Range length (tiles per CTA) of a block-range launch: about `target`
+// tiles, adjusted so that the CTA count is a whole number of waves of
+// `resident` CTAs (CTAs of equal nonzero counts then end together); at least
+// `minPer`.
+inline long long fitted_range(long long tiles, long long target, long long resident, long long minPer) {
+    if (resident < 1) resident = 1;
+    if (target < 1) target = 1;
+    long long waves = (tiles + target * resident - 1) / (target * resident);
+    if (waves < 1) waves = 1;
+    const long long per = (tiles + waves * resident - 1) / (waves * resident);
+    return per < minPer ? minPer : per;
+}
 
 // Reference-compatible partitioning (spmv_csr5.cu:912-925) and search (:497-533).
 spmv_status_t merge_partitions(int numRows, int nnz, int P, int* pos, cudaStream_t s);

@@ -40,13 +40,13 @@ static spmv_variant_t resolve(const spmv_variant_t* req, spmv_type_t type, int R
     if (req) v = *req;
     if (v.kernel == SPMV_KERNEL_HEURISTIC) return heuristic_variant(R, N);
     if (v.kernel == SPMV_KERNEL_AUTO) return auto_variant(type, N);
-    if (!v.blockSize) v.blockSize = 256;
+    if (!v.blockSize) v.blockSize = v.kernel == SPMV_KERNEL_BAND ? 512 : 256;
     if (v.kernel == SPMV_KERNEL_SCALAR) v.threadsPerRow = 1;
     if (v.kernel == SPMV_KERNEL_VECTOR && !v.threadsPerRow) v.threadsPerRow = 32;
     if (v.kernel == SPMV_KERNEL_MERGE && !v.itemsPerThread) v.itemsPerThread = v.vectorWidth == 4 ? 8 : 7;
-    if (v.kernel == SPMV_KERNEL_BAND && !v.itemsPerThread) v.itemsPerThread = 8;
+    if (v.kernel == SPMV_KERNEL_BAND && !v.itemsPerThread) v.itemsPerThread = type == SPMV_TYPE_DOUBLE ? 8 : 16;
     if (v.kernel == SPMV_KERNEL_CSR5 && !v.itemsPerThread) v.itemsPerThread = 4;  // sigma 128
-    if (!v.vectorWidth) v.vectorWidth = 1;
+    if (!v.vectorWidth && v.kernel != SPMV_KERNEL_BAND) v.vectorWidth = 1;  // BAND: 0 = largest window
     return v;
 }
 
@@ -86,8 +86,10 @@ spmv_status_t plan_exec_stream(spmv_plan_t p, T alpha, const T* x, T beta, T* y,
             MXS_TRY(run_merge<T>(merge_geom_of(v), p->mergeTiles, p->merge, a, s, evEnd));
             break;
         case SPMV_KERNEL_BAND:
-            MXS_TRY(run_band<T>(v.blockSize, v.itemsPerThread, p->csr5TileRow, p->csr5Tiles, p->csr5CarryRow,
-                                static_cast<T*>(p->csr5CarryVal), p->errFlag, a, p->numCols, s, evEnd));
+            MXS_TRY(run_band<T>(v.blockSize, v.itemsPerThread, v.threadsPerRow, v.vectorWidth, p->csr5TileRow,
+                                p->csr5Tiles, p->csr5CarryRow, static_cast<T*>(p->csr5CarryVal), p->errFlag, a,
+                                p->numCols, s, evEnd, &p->chains, static_cast<const unsigned*>(p->tileBits),
+                                p->bandTest));
             break;
         case SPMV_KERNEL_CSR5:
             MXS_TRY(run_csr5<T>(32 * v.itemsPerThread, p->csr5TileRow, p->csr5Tiles, p->csr5CarryRow,
@@ -224,14 +226,19 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
     } else if (v.kernel == SPMV_KERNEL_CSR5 || v.kernel == SPMV_KERNEL_BAND) {
         const int sigma = 32 * v.itemsPerThread;
         if (v.kernel == SPMV_KERNEL_CSR5 && v.vectorWidth == 32 &&
-            (v.threadsPerRow > 0 ? (v.blockSize != 256 && v.blockSize != 512 && v.blockSize != 1024)
+            (v.threadsPerRow > 0 ? (v.blockSize != 256 && v.blockSize != 384 && v.blockSize != 512 &&
+                                    v.blockSize != 640 && v.blockSize != 1024)
                                  : (v.blockSize != 128 && v.blockSize != 256 && v.blockSize != 512 &&
                                     v.blockSize != 1024))) {
-            set_error(__FILE__, __LINE__, "ordered CSR5 needs blockSize 128/256/512/1024 (block ranges 256/512/1024), got %d",
+            set_error(__FILE__, __LINE__,
+                      "ordered CSR5 needs blockSize 128/256/512/1024 (block ranges 256/384/512/640/1024), got %d",
                       v.blockSize);
             st = SPMV_ERROR_INTERNAL;
-        } else if (v.kernel == SPMV_KERNEL_BAND && !band_shape_supported(v.blockSize, v.itemsPerThread)) {
-            set_error(__FILE__, __LINE__, "unsupported band shape block=%d ept=%d", v.blockSize, v.itemsPerThread);
+        } else if (v.kernel == SPMV_KERNEL_BAND &&
+                   (!band_shape_supported(v.blockSize, v.itemsPerThread) || v.threadsPerRow < 0 ||
+                    v.vectorWidth < 0)) {
+            set_error(__FILE__, __LINE__, "unsupported band shape block=%d ept=%d tiles/warp=%d window=%dK",
+                      v.blockSize, v.itemsPerThread, v.threadsPerRow, v.vectorWidth);
             st = SPMV_ERROR_INTERNAL;
         } else if (sigma != 128 && sigma != 256 && sigma != 512) {
             set_error(__FILE__, __LINE__, "CSR5 needs itemsPerThread 4, 8 or 16 (sigma 128, 256 or 512)");
@@ -263,9 +270,11 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
                 long long empties = 1;
                 if (st == SPMV_SUCCESS) st = count_empty_rows(rowPtr, R, &empties, h->stream);
                 p->noEmptyRows = st == SPMV_SUCCESS && empties == 0;
-                if (st == SPMV_SUCCESS && v.kernel == SPMV_KERNEL_CSR5)
+                if (st == SPMV_SUCCESS)
                     st = csr5_chains(rowPtr, R, N, sigma, p->csr5TileRow, T, &p->chainBuf, &p->chains, h->stream);
-                if (st == SPMV_SUCCESS && v.kernel == SPMV_KERNEL_CSR5 && v.vectorWidth == 32 && p->noEmptyRows)
+                // ordered tiles (the CSR5 ordered kernels and the x-window kernel) take row-start masks
+                const bool ordered = v.kernel == SPMV_KERNEL_BAND || v.vectorWidth == 32;
+                if (st == SPMV_SUCCESS && ordered && p->noEmptyRows)
                     st = csr5_tile_bits(rowPtr, R, sigma, T, &p->tileBits, h->stream);
                 if (st == SPMV_SUCCESS) {
                     e = cudaStreamSynchronize(h->stream);
@@ -335,8 +344,19 @@ spmv_status_t spmv_plan_device_error(spmv_plan_t p, int* code) {
     *code = h;
     if (h) {
         MXS_CUDA(cudaMemset(p->errFlag, 0, sizeof(int)));
-        MXS_FAIL(SPMV_ERROR_DEVICE, "a pipelined SpMV kernel gave up waiting (code %d); its output is invalid", h);
+        MXS_FAIL(SPMV_ERROR_DEVICE, "an SpMV kernel gave up a bounded wait (code %d); its output is invalid", h);
     }
+    return SPMV_SUCCESS;
+}
+
+spmv_status_t spmv_plan_inject_wait_timeout(spmv_plan_t p, int enable, long long limitCycles) {
+    clear_error();
+    if (!p) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "plan is NULL");
+    if (p->variant.kernel != SPMV_KERNEL_BAND)
+        MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "only BAND plans have a bounded wait to inject into");
+    if (limitCycles < 0) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "negative wait limit");
+    p->bandTest.inject = enable != 0;
+    p->bandTest.waitLimit = enable ? (limitCycles > 0 ? limitCycles : 100000) : 0;
     return SPMV_SUCCESS;
 }
 

@@ -27,7 +27,8 @@ struct spmv_plan_s {
     int* csr5TileOff = nullptr;
     int* csr5CarryRow = nullptr;
     void* csr5CarryVal = nullptr;
-    int* errFlag = nullptr;  // device word raised by a pipelined kernel whose wait gave up
+    int* errFlag = nullptr;  // device word raised by a kernel whose bounded wait gave up
+    mxs::BandTest bandTest{};  // BAND plans: fault injection into the window wait (tests)
     bool noEmptyRows = false;  // checked at plan creation (CSR5 kernels skip the empty-row pass)
     void* chainBuf = nullptr;  // CSR5 carry chains (start / end / row), see Csr5Chains
     void* tileBits = nullptr;  // ordered CSR5 on a matrix without empty rows: row-start masks

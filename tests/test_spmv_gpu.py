@@ -102,8 +102,11 @@ def test_variants_match_oracle(mx, cuda, cases, var, dtype):
             check(y, y0, A, xh, alpha, beta)
 
 
-PLAN_VARIANTS = [("band", 7, 256, 8, 4, 0), ("band", 7, 256, 4, 4, 0), ("band", 7, 512, 8, 4, 0),
-                 ("band", 7, 512, 4, 4, 0), ("csr5_512", 4, 256, 16, 4, 0), ("csr5_128", 4, 256, 4, 4, 0),
+# BAND: (block, ept, window in 1,024-element units, tiles per warp); the
+# 1K and 2K windows leave most gathers of the larger cases outside the window.
+PLAN_VARIANTS = [("band", 7, 512, 16, 0, 0), ("band", 7, 512, 8, 0, 0), ("band", 7, 1024, 16, 0, 2),
+                 ("band", 7, 256, 8, 1, 1), ("band", 7, 256, 16, 2, 3), ("band", 7, 1024, 8, 4, 16),
+                 ("csr5_512", 4, 256, 16, 4, 0), ("csr5_128", 4, 256, 4, 4, 0),
                  ("csr5o_128", 4, 256, 4, 32, 0), ("csr5o_256", 4, 256, 8, 32, 0), ("csr5o_512", 4, 256, 16, 32, 0),
                  ("csr5o_b128", 4, 128, 8, 32, 0), ("csr5o_b512", 4, 512, 8, 32, 0), ("csr5o_b1024", 4, 1024, 8, 32, 0),
                  ("csr5r_256c3", 4, 256, 8, 32, 3), ("csr5r_512c64", 4, 512, 4, 32, 64),
@@ -113,9 +116,9 @@ PLAN_VARIANTS = [("band", 7, 256, 8, 4, 0), ("band", 7, 256, 4, 4, 0), ("band", 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
 @pytest.mark.parametrize("var", PLAN_VARIANTS, ids=[f"{v[0]}b{v[2]}e{v[3]}w{v[4]}" for v in PLAN_VARIANTS])
 def test_plan_variants_match_oracle(mx, cuda, handle, cases, var, dtype):
-    """Plan-only kernels (tile metadata built at plan creation): the windowed
-    persistent kernel, CSR5 at every tile size and block shape, and CSR5
-    block ranges, on every edge case."""
+    """Plan-only kernels (tile metadata built at plan creation): the x-window
+    kernel (large and small windows), CSR5 at every tile size and block shape,
+    and CSR5 block ranges, on every edge case."""
     torch = cuda
     name_, kernel, block, ept, vw, tpr = var
     for name, (rp, ci, v, cols) in cases.items():
@@ -131,6 +134,58 @@ def test_plan_variants_match_oracle(mx, cuda, handle, cases, var, dtype):
             assert p.device_error() == 0
             check(y, y0, A, xh, alpha, beta)
         p.destroy()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_band_unaligned_x_reads_global(mx, cuda, handle, cases, dtype):
+    """x one element past a 16-byte boundary: the window cannot be bulk-copied,
+    so the x-window kernel gathers every column from global memory."""
+    torch = cuda
+    rp, ci, v, cols = cases["powerlaw60k"]
+    A = device_csr(mx, rp, ci, v.astype(dtype), cols)
+    xh = mx.gen_vector(cols, 77, dtype=dtype)
+    xbuf = torch.zeros(cols + 4, dtype=torch.float32 if dtype == np.float32 else torch.float64, device="cuda")
+    x = xbuf[1:cols + 1]
+    x.copy_(torch.from_numpy(xh))
+    assert x.data_ptr() % 16 != 0
+    p = mx.Plan(handle, A, mx.make_variant(mx.KERNEL_BAND, 512, 0, 8, 0))
+    y = torch.empty(A.numRows, dtype=x.dtype, device="cuda")
+    p.exec(x, y)
+    torch.cuda.synchronize()
+    assert p.device_error() == 0
+    check(y, np.zeros(A.numRows, dtype), A, xh, 1.0, 0.0)
+    p.destroy()
+
+
+def test_band_window_wait_runs_out_and_reports(mx, cuda, handle, cases):
+    """The window wait is bounded.  With one arrival of the window barrier
+    held back, every wait runs out after 100,000 clocks; the kernel makes the
+    arrival itself so its bulk copy lands, returns, and the plan reports code 2
+    (SpmvError).  The context stays usable: the next normal execution of the
+    same plan matches the oracle."""
+    torch = cuda
+    rp, ci, v, cols = cases["powerlaw60k"]
+    A = device_csr(mx, rp, ci, v, cols)
+    xh = mx.gen_vector(cols, 77)
+    x = torch.from_numpy(xh).cuda()
+    p = mx.Plan(handle, A, mx.make_variant(mx.KERNEL_BAND, 512, 0, 16, 0))
+    y = torch.zeros(A.numRows, device="cuda")
+    p.inject_wait_timeout(True)
+    p.exec(x, y)
+    torch.cuda.synchronize()
+    with pytest.raises(mx.SpmvError, match="code 2"):
+        p.device_error()
+    assert p.device_error() == 0  # reading the word cleared it
+    p.inject_wait_timeout(False)
+    p.exec(x, y)
+    torch.cuda.synchronize()
+    assert p.device_error() == 0
+    check(y, np.zeros(A.numRows, np.float32), A, xh, 1.0, 0.0)
+    p.destroy()
+    q = mx.Plan(handle, A)  # the default kernel has no bounded wait to inject into
+    with pytest.raises(mx.SpmvError):
+        q.inject_wait_timeout(True)
+    q.destroy()
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
