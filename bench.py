@@ -145,6 +145,14 @@ def make_matrix(mx, W, name, dtype, seed=0, scale_rows=0):
     return spec, rp, ci, v, x, time.time() - t
 
 
+def workload_config(workload, rows, cols, nnz, distinct, nbytes, ws):
+    """The `config` of both arms: what the workload is, nothing about how it
+    is computed (the GPU arm puts its plan under "plan")."""
+    return {"workload": workload, "rows": int(rows), "cols": int(cols), "nnz": int(nnz),
+            "distinct_cols": int(distinct), "algorithmic_bytes": int(nbytes),
+            "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas{ws}"}
+
+
 def cpu_reference_arm(args):
     """The reference's CPU CSR loop on all host threads (oracle port)."""
     import muxi_spmv_gb300 as mx
@@ -172,15 +180,126 @@ def cpu_reference_arm(args):
     val = nbytes * args.steps / tot / 1e9
     line = {"metric": METRIC, "value": round(val, 3), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(tot / args.steps * 1e3, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded)",
+            "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded generators)",
             "impl": "reference",
-            "config": {"workload": args.workload, "rows": spec.numRows, "nnz": int(len(ci)),
-                       "algorithmic_bytes": int(nbytes), "parallelism": "replicas"},
+            "config": workload_config(args.workload, spec.numRows, spec.numCols, int(len(ci)), distinct, nbytes,
+                                      args.gpus),
             "cpu_baseline": {"value": round(val, 3), "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"full {args.workload} matrix, one SpMV pass per step, row-parallel "
-                                       f"reference loop (deep_analysis_runner.cpp:184-190) on {threads} threads"},
+                             "sample": f"full {args.workload} matrix, one SpMV pass per step: the reference's CPU "
+                                       f"CSR loop (deep_analysis_runner.cpp:184-190) restated in oracle/oracle.c, "
+                                       f"row-parallel on {threads} threads; the restatement is pinned bit-exact to "
+                                       f"the reference loop compiled from its sources (tests/test_oracle_pins.py)"},
             "e2e": {"value": round(val, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+SUB_WORKLOADS = (("powerlaw8m", "f64"), ("powerlaw8m_c1024", "f32"), ("stencil2d_4096", "f32"),
+                 ("stencil3d_256", "f32"))
+
+
+def time_plan(torch, plan, x, y, stream, dev, steps, warmup):
+    """(ms per step, ms of the main kernel per launch): CUDA events on the
+    launching stream; the kernel alone from the plan's own event pair."""
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            plan.exec(x, y)
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            plan.exec(x, y)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    step_ms = e0.elapsed_time(e1) / steps
+    plan.profile(True)
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            plan.exec(x, y)
+    km, kl = plan.profile_read()
+    plan.profile(False)
+    return step_ms, km / max(kl, 1)
+
+
+def sub_record(args, mx, W, oracle, h, stream, dev, name, dt, peak):
+    """One compact record of another BASELINE configuration: full-size
+    matrix, the AUTO plan, full-size parity against the FP64 oracle, step
+    and kernel GB/s with the clocks sampled during the timed region."""
+    import torch
+    dtype = np.float32 if dt == "f32" else np.float64
+    vs = np.dtype(dtype).itemsize
+    spec, rp, ci, v, xh, gen_s = make_matrix(mx, W, name, dtype, seed=0)
+    A = mx.CSRMatrix(rp, ci, v, spec.numCols).copyToDevice(dev)
+    plan = mx.Plan(h, A)
+    distinct = mx.count_distinct_columns(A, stream)
+    nbytes = algorithmic_bytes(A.numRows, A.nnz, distinct, vs)
+    x = torch.from_numpy(xh).to(dev)
+    y = torch.empty(A.numRows, dtype=x.dtype, device=dev)
+    with torch.cuda.stream(stream):
+        plan.exec(x, y)
+    stream.synchronize()
+    plan.device_error()
+    y_ref, absum = oracle.spmv_ref(rp, ci, v, xh)
+    r = oracle.row_errors(y.cpu().numpy(), y_ref, absum, 1e-5 if dtype == np.float32 else 1e-13)
+    clocks = ClockSampler(dev.index or 0)
+    clocks.start()
+    time.sleep(0.3)
+    step_ms, kern_ms = time_plan(torch, plan, x, y, stream, dev, args.steps, args.warmup)
+    clocks.stop()
+    pv = plan.variant.as_dict()
+    rec = {"workload": name, "dtype": dt, "rows": A.numRows, "nnz": A.nnz, "algorithmic_bytes": int(nbytes),
+           "variant": pv, "ms_per_step": round(step_ms, 5), "value": round(nbytes / (step_ms * 1e-3) / 1e9, 3),
+           "kernel_ms": round(kern_ms, 5), "kernel_GBps": round(nbytes / (kern_ms * 1e-3) / 1e9, 2),
+           "frac": round(nbytes / (kern_ms * 1e-3) / 1e9 / peak, 4),
+           "parity": {"rows_checked": int(A.numRows), "max_err_over_bound": float(r.max()),
+                      "rows_out_of_bound": int((r > 1).sum())},
+           "clocks": clocks.summary(), "generate_s": round(gen_s, 2)}
+    if rec["parity"]["rows_out_of_bound"]:
+        print(f"PARITY FAILURE {name} {dt}: {rec['parity']}", file=sys.stderr)
+    plan.destroy()
+    del A, x, y
+    torch.cuda.empty_cache()
+    return rec
+
+
+def selector_record(args, mx, h, A, x, y, stream, dev):
+    """The learned kernel pick against the exhaustive autotune on one matrix:
+    regret of the pick's time and the ratio of the two selections' costs."""
+    import torch
+    from muxi_spmv_gb300 import selector as S
+    model = S.MLP.load(S.DEFAULT_MODEL)
+    space = S.variant_space()
+    torch.cuda.synchronize(dev)
+    S.select(h, A, S.SELECT_LEARNED, model)  # warm: feature buffers, model upload
+    torch.cuda.synchronize(dev)
+    t = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        learned, li = S.select(h, A, S.SELECT_LEARNED, model)
+    torch.cuda.synchronize(dev)
+    learned_s = (time.perf_counter() - t) / reps
+    t = time.perf_counter()
+    best, bi = S.select(h, A, S.SELECT_AUTOTUNE)
+    torch.cuda.synchronize(dev)
+    autotune_s = time.perf_counter() - t
+    times = {}
+    for tag, var in (("learned", learned), ("autotune", best)):
+        p = mx.Plan(h, A, var)
+        step_ms, _ = time_plan(torch, p, x, y, stream, dev, args.steps, args.warmup)
+        times[tag] = step_ms
+        p.destroy()
+    model.destroy()
+    return {"matrix": args.workload, "learned_pick": S.variant_name(space[li]) if li >= 0 else str(learned),
+            "autotune_pick": S.variant_name(space[bi]) if bi >= 0 else str(best),
+            "learned_ms": round(times["learned"], 5), "autotune_ms": round(times["autotune"], 5),
+            "regret": round(times["learned"] / times["autotune"] - 1.0, 4),
+            "selection_ms": {"learned": round(learned_s * 1e3, 3), "autotune": round(autotune_s * 1e3, 3)},
+            "cost_ratio": round(autotune_s / max(learned_s, 1e-9), 1),
+            "note": "selection = spmv_select (features + MLP forward + rank) vs spmv_select(AUTOTUNE) "
+                    "(every applicable variant timed as a plan); regret from both picks' plans timed "
+                    "back to back with CUDA events"}
 
 
 def gpu_arm(args):
@@ -428,12 +547,10 @@ def gpu_arm(args):
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(step_ms, 5), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded generators)",
-            "config": {"workload": args.workload + (f"+colperm_{args.colperm}" if perm is not None else ""),
-                       "rows": A.numRows, "cols": A.numCols, "nnz": A.nnz,
-                       "distinct_cols": distinct, "algorithmic_bytes": int(nbytes), "variant": pv,
-                       "select": "explicit variant" if args.variant else args.select,
-                       "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas{ws}",
-                       "gflops": round(2 * A.nnz / (step_ms * 1e-3) / 1e9, 2), "generate_s": round(gen_s, 2)},
+            "config": workload_config(args.workload + (f"+colperm_{args.colperm}" if perm is not None else ""),
+                                      A.numRows, A.numCols, A.nnz, distinct, nbytes, ws),
+            "plan": {"variant": pv, "select": "explicit variant" if args.variant else args.select,
+                     "gflops": round(2 * A.nnz / (step_ms * 1e-3) / 1e9, 2), "generate_s": round(gen_s, 2)},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                          "kernel": kern_names.get(pv["kernel"], str(pv["kernel"])),
@@ -464,11 +581,26 @@ def gpu_arm(args):
         ser_s = time.perf_counter() - t
         line["cpu_baseline"] = {"value": round(nbytes / cpu_s / 1e9, 3), "unit": UNIT, "cores": threads,
                                 "kind": "port",
-                                "sample": f"full matrix, {reps} row-parallel passes of the reference CPU loop",
+                                "sample": f"full matrix, {reps} row-parallel passes of the reference's CPU CSR loop "
+                                          "(deep_analysis_runner.cpp:184-190) restated in oracle/oracle.c, which is "
+                                          "pinned bit-exact to that loop compiled from the reference's sources "
+                                          "(tests/test_oracle_pins.py)",
                                 "serial_value": round(nbytes / ser_s / 1e9, 3), "serial_cores": 1}
+    if rank == 0 and not args.no_subrecords and not args.scale_rows and perm is None:
+        # the other configurations, each through its own AUTO plan, and the
+        # learned selector on this matrix (outside the headline's timed region)
+        if dtype == np.float32:
+            line["selector"] = selector_record(args, mx, h, A, x, y, stream, dev)
+        plan.destroy()
+        plan = None
+        del A, x, y, x0
+        torch.cuda.empty_cache()
+        line["subrecords"] = [sub_record(args, mx, W, oracle, h, stream, dev, name, dt, peak)
+                              for name, dt in SUB_WORKLOADS if (name, dt) != (args.workload, args.dtype)]
     if rank == 0:
         print(json.dumps(line), flush=True)
-    plan.destroy()
+    if plan is not None:
+        plan.destroy()
     h.destroy()
     if ws > 1:
         dist.destroy_process_group()
@@ -742,6 +874,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-pipeline", action="store_true", help="e2e through one stream, copies not overlapped")
     ap.add_argument("--no-vendor", action="store_true", help="skip the cuSPARSE comparison")
+    ap.add_argument("--no-subrecords", action="store_true",
+                    help="skip the other configurations and the selector record (profiling runs)")
     ap.add_argument("--select", default="default", choices=["default", "learned"],
                     help="AUTO plan: the fixed default variant, or the learned selector's pick")
     ap.add_argument("--slices", type=int, default=1, help="host pipeline row slices")

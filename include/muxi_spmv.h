@@ -225,19 +225,24 @@ SPMV_API spmv_status_t spmv_bsr_f64(int numRows, int numCols, int B, int numBloc
                                     double alpha, double beta, cudaStream_t stream);
 
 /* FP32 CSR SpMV that allocates no device memory (no counterpart in the
- * reference).  Same kernels and results as spmv_csr_f32 (default merge-path
- * variant), for callers that cannot allocate: code recording a CUDA graph,
- * code running under a device-memory budget owned by another allocator, or
- * a real-time loop that must not pay an allocation or the synchronisation it
+ * reference).  It runs the kernels of spmv_csr_f32 given the SPMV_KERNEL_MERGE
+ * variant {256, 0, 8, 4} (merge-path tiles plus carry fix-up; a default
+ * spmv_csr_f32 call runs CSR5 tiles instead, so the two agree within the FP32
+ * row bound, not bit for bit).  It is for callers that cannot allocate:
+ * code running under a device-memory budget owned by another allocator, or a
+ * real-time loop that must not pay an allocation or the synchronisation it
  * can cause.  The caller passes inputs and outputs; the scratch (tile
  * coordinates and carries) is a fixed 8 MiB device array inside the library,
- * so numRows + nnz may reach about 1.07e9 -- larger matrices are rejected with
- * SPMV_ERROR_MEMORY_ALLOC and a message.  Every GPU that loads the library
- * keeps that array until the process exits.  The first call on a device
- * looks up the array's address (cudaGetSymbolAddress); make it before any
- * stream capture.  All calls share the one array: calls that can overlap on
- * the GPU (different streams without ordering) race and must be serialised
- * by the caller. */
+ * so numRows + nnz may reach about 1.07e9 when colIdx and values are 16-byte
+ * aligned and about 0.94e9 otherwise -- larger matrices are rejected with
+ * SPMV_ERROR_MEMORY_ALLOC and a message that states the limit.  Every GPU
+ * that loads the library keeps that array until the process exits.  The
+ * first call on a device looks up the array's address (cudaGetSymbolAddress)
+ * and keeps it; make that call before any stream capture, and do not use the
+ * entry point on a device after cudaDeviceReset.  All calls share the one
+ * array, which keeps the last call's contents (nothing in it needs to start
+ * at zero): calls that can overlap on the GPU (different streams without
+ * ordering) race and must be serialised by the caller. */
 SPMV_API spmv_status_t spmv_csr_noalloc_f32(int numRows, int numCols, int nnz,
                                             const int* rowPtr, const int* colIdx, const float* values,
                                             const float* x, float* y, float alpha, float beta,
@@ -515,6 +520,19 @@ SPMV_API spmv_status_t spmv_plan_device_error(spmv_plan_t plan, int* code);
  * stays usable.  enable = 0 restores normal executions.  Plans of other
  * kernels have no waits: SPMV_ERROR_UNSUPPORTED_FORMAT. */
 SPMV_API spmv_status_t spmv_plan_inject_wait_timeout(spmv_plan_t plan, int enable, long long limitCycles);
+
+/* Device-memory accounting and allocation-failure injection for tests (no
+ * reference counterpart; the reference's status contract,
+ * src/utils/common.h:31-43, names SPMV_ERROR_MEMORY_ALLOC but nothing raises
+ * it).  Every device allocation the library makes -- plans, pipelines,
+ * batches, selector models, stateless scratch -- is counted while live:
+ * spmv_debug_device_memory reports the live bytes and allocations.
+ * spmv_debug_fail_allocation(n), n >= 1: the n-th device allocation from now
+ * fails as if the device were out of memory (the driver is not asked); the
+ * call that made it returns SPMV_ERROR_MEMORY_ALLOC after releasing what it
+ * had taken.  n = 0 turns injection off.  Process-wide, not thread-local. */
+SPMV_API spmv_status_t spmv_debug_fail_allocation(long long n);
+SPMV_API spmv_status_t spmv_debug_device_memory(long long* liveBytes, long long* liveAllocations);
 
 /* Kernel timing on the launching stream (the role of the reference's
  * GpuTimer, src/utils/timer.h:17-47, moved into the plan): while enabled,

@@ -151,6 +151,8 @@ SIGNATURES = {
     "spmv_plan_exec_op_f64": (S, [C.POINTER(Handle), P, I, D, P, D, P]),
     "spmv_plan_device_error": (S, [P, C.POINTER(C.c_int)]),
     "spmv_plan_inject_wait_timeout": (S, [P, I, C.c_longlong]),
+    "spmv_debug_fail_allocation": (S, [C.c_longlong]),
+    "spmv_debug_device_memory": (S, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "spmv_plan_profile": (S, [P, I]),
     "spmv_plan_profile_read": (S, [P, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "spmv_count_distinct_columns": (S, [I, I, P, C.POINTER(C.c_longlong), P]),

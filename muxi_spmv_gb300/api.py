@@ -263,6 +263,19 @@ def csr_transpose(A: CSRMatrix, stream=None) -> CSRMatrix:
     return B
 
 
+def debug_fail_allocation(n: int):
+    """Tests: the n-th device allocation of the library from now fails as out
+    of memory (0 turns this off); see spmv_debug_fail_allocation."""
+    check(lib().spmv_debug_fail_allocation(int(n)), "spmv_debug_fail_allocation")
+
+
+def debug_device_memory() -> tuple[int, int]:
+    """(live bytes, live allocations) of the library's device memory."""
+    b, n = C.c_longlong(), C.c_longlong()
+    check(lib().spmv_debug_device_memory(C.byref(b), C.byref(n)), "spmv_debug_device_memory")
+    return b.value, n.value
+
+
 def make_variant(kernel: int, blockSize: int = 256, threadsPerRow: int = 0, itemsPerThread: int = 0,
                  vectorWidth: int = 1) -> Variant:
     return Variant(kernel, blockSize, threadsPerRow, itemsPerThread, vectorWidth)

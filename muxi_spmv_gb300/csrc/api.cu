@@ -32,7 +32,7 @@ void clear_error() { g_err[0] = 0; }
 
 spmv_status_t cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
     set_error(file, line, "CUDA error in %s: %s", what, cudaGetErrorString(e));
-    return SPMV_ERROR_DEVICE;
+    return e == cudaErrorMemoryAllocation ? SPMV_ERROR_MEMORY_ALLOC : SPMV_ERROR_DEVICE;
 }
 
 // ---------------------------------------------------------------------------
@@ -100,7 +100,7 @@ spmv_status_t scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
     cudaMemPool_t pool;
     MXS_TRY(pool_for_current(&pool));
     if (bytes == 0) bytes = 256;
-    cudaError_t e = cudaMallocFromPoolAsync(p, bytes, pool, s);
+    cudaError_t e = dev_malloc_pool_async(p, bytes, pool, s);
     if (e != cudaSuccess) {
         set_error(__FILE__, __LINE__, "scratch allocation of %zu bytes failed: %s", bytes,
                   cudaGetErrorString(e));
@@ -111,7 +111,7 @@ spmv_status_t scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
 
 spmv_status_t scratch_free(void* p, cudaStream_t s) {
     if (!p) return SPMV_SUCCESS;
-    MXS_CUDA(cudaFreeAsync(p, s));
+    MXS_CUDA(dev_free_async(p, s));
     return SPMV_SUCCESS;
 }
 

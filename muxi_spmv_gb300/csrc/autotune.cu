@@ -72,10 +72,10 @@ static spmv_status_t tune(spmv_handle_t* h, spmv_type_t type, int R, int C, int 
     const cudaStream_t s = h->stream;
     T* x = nullptr;
     T* y = nullptr;
-    MXS_CUDA(cudaMalloc(&x, sizeof(T) * (size_t)(C > 0 ? C : 1)));
-    cudaError_t e = cudaMalloc(&y, sizeof(T) * (size_t)(R > 0 ? R : 1));
+    MXS_CUDA(dev_malloc(&x, sizeof(T) * (size_t)(C > 0 ? C : 1)));
+    cudaError_t e = dev_malloc(&y, sizeof(T) * (size_t)(R > 0 ? R : 1));
     if (e != cudaSuccess) {
-        cudaFree(x);
+        dev_free(x);
         return cuda_fail(e, "autotune buffers", __FILE__, __LINE__);
     }
     fill_kernel_t<T><<<256, 256, 0, s>>>(C, x, T(1));
@@ -137,8 +137,8 @@ static spmv_status_t tune(spmv_handle_t* h, spmv_type_t type, int R, int C, int 
             break;
         }
     }
-    cudaFree(x);
-    cudaFree(y);
+    dev_free(x);
+    dev_free(y);
     if (best) *best = bestIdx;
     if (result != SPMV_SUCCESS) MXS_FAIL(result, "autotune aborted on a device error");
     if (bestIdx < 0) MXS_FAIL(SPMV_ERROR_INTERNAL, "no variant could run on this matrix");

@@ -510,10 +510,10 @@ spmv_status_t spmv_batch_destroy(spmv_batch_t b) {
     for (auto& g : b->graph)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     if (b->capStream) cudaStreamDestroy(b->capStream);
-    cudaFree(b->dDesc);
-    cudaFree(b->dTileStart);
-    cudaFree(b->dTileRow);
-    cudaFree(b->dCarryRow);
+    dev_free(b->dDesc);
+    dev_free(b->dTileStart);
+    dev_free(b->dTileRow);
+    dev_free(b->dCarryRow);
     delete b;
     return SPMV_SUCCESS;
 }
@@ -582,19 +582,19 @@ spmv_status_t spmv_batch_create_ex(spmv_handle_t* h, int count, const spmv_batch
     const cudaStream_t s = h->stream;
     int* tileOff = nullptr;
     spmv_status_t st = SPMV_SUCCESS;
-    cudaError_t e = cudaMalloc(&b->dDesc, sizeof(BatchDesc) * count);
-    if (e == cudaSuccess) e = cudaMalloc(&b->dTileStart, sizeof(int) * (count + 1));
-    if (e == cudaSuccess) e = cudaMalloc(&b->dTileRow, sizeof(int) * tiles);
-    if (e == cudaSuccess) e = cudaMalloc(&tileOff, sizeof(int) * tiles);
+    cudaError_t e = dev_malloc(&b->dDesc, sizeof(BatchDesc) * count);
+    if (e == cudaSuccess) e = dev_malloc(&b->dTileStart, sizeof(int) * (count + 1));
+    if (e == cudaSuccess) e = dev_malloc(&b->dTileRow, sizeof(int) * tiles);
+    if (e == cudaSuccess) e = dev_malloc(&tileOff, sizeof(int) * tiles);
     // carries: row, matrix, k values per chunk
     // persistent chunks, or at most one full-GPU grid of chunks per matrix
     size_t nch = (size_t)((tiles + b->chunkTiles - 1) / b->chunkTiles);
     if (nch < (size_t)b->warps) nch = (size_t)b->warps;
     const size_t rowsBytes = (sizeof(int) * 2 * nch + 255) & ~size_t(255);
     const size_t cb = rowsBytes + sizeof(float) * k * nch;
-    if (e == cudaSuccess) e = cudaMalloc(&b->dCarryRow, cb);
+    if (e == cudaSuccess) e = dev_malloc(&b->dCarryRow, cb);
     if (e != cudaSuccess) {
-        cudaFree(tileOff);
+        dev_free(tileOff);
         spmv_batch_destroy(b);
         return cuda_fail(e, "batch allocation", __FILE__, __LINE__);
     }
@@ -613,7 +613,7 @@ spmv_status_t spmv_batch_create_ex(spmv_handle_t* h, int count, const spmv_batch
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) st = cuda_fail(e, "batch setup", __FILE__, __LINE__);
     }
-    cudaFree(tileOff);
+    dev_free(tileOff);
     if (st != SPMV_SUCCESS) {
         spmv_batch_destroy(b);
         return st;

@@ -62,7 +62,7 @@ spmv_status_t csr5_tile_bits(const int* rowPtr, int numRows, int sigma, long lon
     if (tiles <= 0) return SPMV_SUCCESS;
     const int words = sigma / 32;
     const size_t bytes = sizeof(unsigned) * (size_t)tiles * words;
-    MXS_CUDA(cudaMalloc(buf, bytes));
+    MXS_CUDA(dev_malloc(buf, bytes));
     cudaError_t e = cudaMemsetAsync(*buf, 0, bytes, s);
     if (e == cudaSuccess) {
         tile_bits_kernel<<<grid_for(numRows > 0 ? numRows : 1, 256), 256, 0, s>>>(rowPtr, numRows, sigma, words,
@@ -71,7 +71,7 @@ spmv_status_t csr5_tile_bits(const int* rowPtr, int numRows, int sigma, long lon
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
-        cudaFree(*buf);
+        dev_free(*buf);
         *buf = nullptr;
         return cuda_fail(e, "tile row masks", __FILE__, __LINE__);
     }
@@ -203,7 +203,7 @@ spmv_status_t csr5_chains(const int* rowPtr, int numRows, int nnz, int sigma, co
         if (e != cudaSuccess) st = cuda_fail(e, "carry chains", __FILE__, __LINE__);
     }
     if (st == SPMV_SUCCESS && n > 0) {
-        cudaError_t e = cudaMalloc(buf, 3 * sizeof(int) * (size_t)n);
+        cudaError_t e = dev_malloc(buf, 3 * sizeof(int) * (size_t)n);
         if (e != cudaSuccess) {
             *buf = nullptr;
             st = cuda_fail(e, "carry chain table", __FILE__, __LINE__);
@@ -221,7 +221,7 @@ spmv_status_t csr5_chains(const int* rowPtr, int numRows, int nnz, int sigma, co
     }
     scratch_free(tmp, s);
     if (st != SPMV_SUCCESS) {
-        if (*buf) cudaFree(*buf);
+        if (*buf) dev_free(*buf);
         *buf = nullptr;
         out->n = -1;
         return st;

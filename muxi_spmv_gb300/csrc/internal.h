@@ -37,6 +37,22 @@ struct HandleState {
     spmv_select_mode_t selectorMode = SPMV_SELECT_LEARNED;  // or SPMV_SELECT_LEARNED_FALLBACK
 };
 
+// Device allocations of the library (device_memory.cu): counted while live,
+// and failable on demand for tests (spmv_debug_fail_allocation).
+cudaError_t dev_malloc(void** p, size_t bytes);
+template <typename T>
+inline cudaError_t dev_malloc(T** p, size_t bytes) {
+    return dev_malloc(reinterpret_cast<void**>(p), bytes);
+}
+cudaError_t dev_free(void* p);
+cudaError_t dev_malloc_async(void** p, size_t bytes, cudaStream_t s);
+template <typename T>
+inline cudaError_t dev_malloc_async(T** p, size_t bytes, cudaStream_t s) {
+    return dev_malloc_async(reinterpret_cast<void**>(p), bytes, s);
+}
+cudaError_t dev_malloc_pool_async(void** p, size_t bytes, cudaMemPool_t pool, cudaStream_t s);
+cudaError_t dev_free_async(void* p, cudaStream_t s);
+
 // Per-device properties cached on first use (SM count, L2 size, smem).
 struct DeviceProps {
     int sm_count = 0;

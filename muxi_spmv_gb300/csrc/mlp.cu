@@ -157,10 +157,10 @@ struct Work {
 spmv_status_t ensure_work(spmv_mlp_s* n, int B, Work& w) {
     const size_t per = (size_t)n->in + n->h1 + n->h2 + 2 * (size_t)n->out + n->h2 + n->h1;
     if (B > n->cap) {
-        if (n->work) cudaFree(n->work);
+        if (n->work) dev_free(n->work);
         n->work = nullptr;
         n->cap = 0;
-        MXS_CUDA(cudaMalloc(&n->work, sizeof(float) * per * (size_t)B));
+        MXS_CUDA(dev_malloc(&n->work, sizeof(float) * per * (size_t)B));
         n->cap = B;
     }
     float* p = n->work;
@@ -258,14 +258,14 @@ extern "C" {
 spmv_status_t spmv_mlp_destroy(spmv_mlp_t n) {
     clear_error();
     if (!n) MXS_FAIL(SPMV_ERROR_INVALID_HANDLE, "model is NULL");
-    cudaFree(n->params);
-    cudaFree(n->grads);
-    cudaFree(n->m);
-    cudaFree(n->v);
-    cudaFree(n->mean);
-    cudaFree(n->stdv);
-    cudaFree(n->work);
-    cudaFree(n->lossAcc);
+    dev_free(n->params);
+    dev_free(n->grads);
+    dev_free(n->m);
+    dev_free(n->v);
+    dev_free(n->mean);
+    dev_free(n->stdv);
+    dev_free(n->work);
+    dev_free(n->lossAcc);
     delete n;
     return SPMV_SUCCESS;
 }
@@ -284,13 +284,13 @@ spmv_status_t spmv_mlp_create(int in, int h1, int h2, int out, unsigned long lon
     n->out = out;
     n->nparams = h1 * in + h1 + h2 * h1 + h2 + out * h2 + out;
     const size_t pb = sizeof(float) * n->nparams;
-    cudaError_t e = cudaMalloc(&n->params, pb);
-    if (e == cudaSuccess) e = cudaMalloc(&n->grads, pb);
-    if (e == cudaSuccess) e = cudaMalloc(&n->m, pb);
-    if (e == cudaSuccess) e = cudaMalloc(&n->v, pb);
-    if (e == cudaSuccess) e = cudaMalloc(&n->mean, sizeof(float) * in);
-    if (e == cudaSuccess) e = cudaMalloc(&n->stdv, sizeof(float) * in);
-    if (e == cudaSuccess) e = cudaMalloc(&n->lossAcc, 2 * sizeof(float));
+    cudaError_t e = dev_malloc(&n->params, pb);
+    if (e == cudaSuccess) e = dev_malloc(&n->grads, pb);
+    if (e == cudaSuccess) e = dev_malloc(&n->m, pb);
+    if (e == cudaSuccess) e = dev_malloc(&n->v, pb);
+    if (e == cudaSuccess) e = dev_malloc(&n->mean, sizeof(float) * in);
+    if (e == cudaSuccess) e = dev_malloc(&n->stdv, sizeof(float) * in);
+    if (e == cudaSuccess) e = dev_malloc(&n->lossAcc, 2 * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(n->m, 0, pb);
     if (e == cudaSuccess) e = cudaMemset(n->v, 0, pb);
     if (e != cudaSuccess) {

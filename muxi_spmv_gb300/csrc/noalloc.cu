@@ -1,15 +1,19 @@
-// spmv_csr_noalloc_f32: the stateless FP32 CSR SpMV (merge-path tiles plus
-// carry fix-up, the kernels of spmv_csr_f32) for callers that must not
-// allocate device memory.  Examples: code recording a CUDA graph or running
-// under a strict device-memory budget owned by another allocator, a
-// real-time loop where an allocation (and the synchronisation it can cause)
-// is not allowed, or a library callback that has no allocator handed to it.
+// spmv_csr_noalloc_f32: a stateless FP32 CSR SpMV (merge-path tiles plus
+// carry fix-up: spmv_csr_f32's kernels when that call is given the
+// SPMV_KERNEL_MERGE variant {256, 0, 8, 4}) for callers that must not
+// allocate device memory.  Examples: code running under a strict
+// device-memory budget owned by another allocator, a real-time loop where an
+// allocation (and the synchronisation it can cause) is not allowed, or a
+// library callback that has no allocator handed to it.
 //
 // The tile coordinates and carries live in one file-scope device array of
 // kNoAllocScratchBytes.  Every GPU that loads this library reserves that
 // array for the life of the process.  Its device address is looked up with
 // cudaGetSymbolAddress once per device, on the first call made with that
-// device current; make that first call before any stream capture.
+// device current; make that first call before any stream capture.  The
+// address stays cached for the process: after a cudaDeviceReset the module is
+// reloaded and the array may move, so do not call this entry point on a
+// device that has been reset.
 #include <mutex>
 #include <vector>
 
@@ -19,9 +23,17 @@
 namespace mxs {
 namespace {
 
-// 8 MiB: 16 bytes per merge tile (plus alignment), so about 520,000 tiles of
-// 2,044 rows+nonzeros, i.e. numRows + nnz up to about 1.07e9.
+// 8 MiB: 16 bytes per merge tile (plus alignment), so up to 524,224 tiles:
+// numRows + nnz up to about 1.07e9 with 16-byte-aligned colIdx / values
+// (2,044-item tiles), about 0.94e9 otherwise (1,792-item tiles).
 constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;
+
+// Largest numRows + nnz the array serves with tiles of geometry g.
+long long max_items(const MergeGeom& g) {
+    long long P = (long long)(kNoAllocScratchBytes / 16);
+    while (P > 1 && merge_scratch_bytes(P, sizeof(float)) > kNoAllocScratchBytes) --P;
+    return P * g.tile();
+}
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 std::mutex g_mu;
@@ -60,8 +72,8 @@ extern "C" spmv_status_t spmv_csr_noalloc_f32(int numRows, int numCols, int nnz,
     if (need > kNoAllocScratchBytes)
         MXS_FAIL(SPMV_ERROR_MEMORY_ALLOC,
                  "matrix needs %zu bytes of scratch (%lld merge tiles); the no-allocation entry point has a fixed "
-                 "%zu-byte array (numRows + nnz up to about 1.07e9)",
-                 need, tiles, kNoAllocScratchBytes);
+                 "%zu-byte array (numRows + nnz up to %lld for this call's colIdx / values alignment)",
+                 need, tiles, kNoAllocScratchBytes, max_items(g));
     if (numRows > 0 && (!rowPtr || !y)) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "rowPtr or y is NULL");
     if (nnz > 0 && (!colIdx || !values || !x)) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "colIdx, values or x is NULL");
     if (numRows == 0) return SPMV_SUCCESS;

@@ -97,9 +97,9 @@ static void pipeline_free(spmv_pipeline_t p) {
         if (e) cudaEventDestroy(e);
     for (cudaStream_t s : {p->sIn, p->sOut, p->sComp[0], p->sComp[1]})
         if (s) cudaStreamDestroy(s);
-    if (p->rebased) cudaFree(p->rebased);
-    if (p->xbuf) cudaFree(p->xbuf);
-    if (p->ybuf) cudaFree(p->ybuf);
+    if (p->rebased) dev_free(p->rebased);
+    if (p->xbuf) dev_free(p->xbuf);
+    if (p->ybuf) dev_free(p->ybuf);
     delete p;
 }
 
@@ -117,12 +117,12 @@ static spmv_status_t pipeline_build(spmv_handle_t* h, spmv_pipeline_t p, const i
     std::vector<int> rows(S + 1), nz(S + 1);
     if (R > 0) {
         int* d = nullptr;
-        MXS_CUDA(cudaMallocAsync(&d, 2 * sizeof(int) * (S + 1), hs));
+        MXS_CUDA(dev_malloc_async(&d, 2 * sizeof(int) * (S + 1), hs));
         slice_bounds_kernel<<<grid_for(S + 1, 128), 128, 0, hs>>>(rowPtr, R, N, S, d, d + S + 1);
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaMemcpyAsync(rows.data(), d, sizeof(int) * (S + 1), cudaMemcpyDeviceToHost, hs);
         if (e == cudaSuccess) e = cudaMemcpyAsync(nz.data(), d + S + 1, sizeof(int) * (S + 1), cudaMemcpyDeviceToHost, hs);
-        cudaFreeAsync(d, hs);
+        dev_free_async(d, hs);
         if (e == cudaSuccess) e = cudaStreamSynchronize(hs);
         if (e != cudaSuccess) return cuda_fail(e, "pipeline slice bounds", __FILE__, __LINE__);
     }
@@ -140,7 +140,7 @@ static spmv_status_t pipeline_build(spmv_handle_t* h, spmv_pipeline_t p, const i
     // Rebased rowPtr of every slice, then one plan per slice.
     if (slices > 0) {
         const size_t total = (size_t)R + slices;
-        MXS_CUDA(cudaMalloc(&p->rebased, sizeof(int) * total));
+        MXS_CUDA(dev_malloc(&p->rebased, sizeof(int) * total));
         p->deviceBytes += sizeof(int) * total;
         size_t off = 0;
         for (int s = 0; s < slices; ++s) {
@@ -163,8 +163,8 @@ static spmv_status_t pipeline_build(spmv_handle_t* h, spmv_pipeline_t p, const i
 
     // Device x / y per slot and the events that order the slots.
     const size_t xb = ((vs * (size_t)C) + 255) & ~size_t(255), yb = ((vs * (size_t)R) + 255) & ~size_t(255);
-    if (xb) MXS_CUDA(cudaMalloc(&p->xbuf, xb * p->depth));
-    if (yb) MXS_CUDA(cudaMalloc(&p->ybuf, yb * p->depth));
+    if (xb) MXS_CUDA(dev_malloc(&p->xbuf, xb * p->depth));
+    if (yb) MXS_CUDA(dev_malloc(&p->ybuf, yb * p->depth));
     p->deviceBytes += (xb + yb) * p->depth;
     auto mk = [](cudaEvent_t* e) { return cudaEventCreateWithFlags(e, cudaEventDisableTiming); };
     p->evIn.assign(p->depth, nullptr);

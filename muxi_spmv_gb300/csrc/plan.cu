@@ -208,7 +208,7 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
         } else if (R > 0 && N > 0) {
             p->mergeTiles = merge_tile_count(R, N, g);
             const size_t bytes = merge_scratch_bytes(p->mergeTiles, vs);
-            cudaError_t e = cudaMalloc(&p->mergeBuf, bytes);
+            cudaError_t e = dev_malloc(&p->mergeBuf, bytes);
             if (e != cudaSuccess) {
                 set_error(__FILE__, __LINE__, "plan allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
                 st = SPMV_ERROR_MEMORY_ALLOC;
@@ -251,7 +251,7 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
             const size_t a4 = ((sizeof(int) * T) + 255) & ~size_t(255);
             const size_t av = ((vs * T) + 255) & ~size_t(255);
             const size_t bytes = 3 * a4 + av + 256;  // + the device error word
-            cudaError_t e = cudaMalloc(&p->csr5Buf, bytes);
+            cudaError_t e = dev_malloc(&p->csr5Buf, bytes);
             if (e != cudaSuccess) {
                 set_error(__FILE__, __LINE__, "plan allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
                 st = SPMV_ERROR_MEMORY_ALLOC;
@@ -294,7 +294,7 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
             const size_t slots = (size_t)R * W;
             const size_t a4 = (sizeof(int) * slots + 255) & ~size_t(255);
             const size_t bytes = a4 + vs * slots;
-            cudaError_t e = cudaMalloc(&p->ellBuf, bytes);
+            cudaError_t e = dev_malloc(&p->ellBuf, bytes);
             if (e != cudaSuccess) {
                 set_error(__FILE__, __LINE__, "plan allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
                 st = SPMV_ERROR_MEMORY_ALLOC;
@@ -322,11 +322,11 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
         st = SPMV_ERROR_UNSUPPORTED_FORMAT;
     }
     if (st != SPMV_SUCCESS) {
-        if (p->mergeBuf) cudaFree(p->mergeBuf);
-        if (p->csr5Buf) cudaFree(p->csr5Buf);
-        if (p->chainBuf) cudaFree(p->chainBuf);
-        if (p->tileBits) cudaFree(p->tileBits);
-        if (p->ellBuf) cudaFree(p->ellBuf);
+        if (p->mergeBuf) dev_free(p->mergeBuf);
+        if (p->csr5Buf) dev_free(p->csr5Buf);
+        if (p->chainBuf) dev_free(p->chainBuf);
+        if (p->tileBits) dev_free(p->tileBits);
+        if (p->ellBuf) dev_free(p->ellBuf);
         delete p;
         return st;
     }
@@ -391,14 +391,14 @@ spmv_status_t spmv_plan_destroy(spmv_plan_t p) {
         cudaEventDestroy(e.first);
         cudaEventDestroy(e.second);
     }
-    if (p->mergeBuf) cudaFree(p->mergeBuf);
-    if (p->csr5Buf) cudaFree(p->csr5Buf);
-    if (p->chainBuf) cudaFree(p->chainBuf);
-    if (p->tileBits) cudaFree(p->tileBits);
-    if (p->ellBuf) cudaFree(p->ellBuf);
-    if (p->ownedCsr) cudaFree(p->ownedCsr);
+    if (p->mergeBuf) dev_free(p->mergeBuf);
+    if (p->csr5Buf) dev_free(p->csr5Buf);
+    if (p->chainBuf) dev_free(p->chainBuf);
+    if (p->tileBits) dev_free(p->tileBits);
+    if (p->ellBuf) dev_free(p->ellBuf);
+    if (p->ownedCsr) dev_free(p->ownedCsr);
     if (p->tPlan) spmv_plan_destroy(p->tPlan);
-    if (p->tBuf) cudaFree(p->tBuf);
+    if (p->tBuf) dev_free(p->tBuf);
     delete p;
     return SPMV_SUCCESS;
 }
@@ -420,7 +420,7 @@ spmv_status_t spmv_plan_create_ex(spmv_handle_t* h, spmv_type_t type, int R, int
     const size_t a0 = (sizeof(int) * ((size_t)R + 1) + 255) & ~size_t(255);
     const size_t a1 = (sizeof(int) * (size_t)N + 255) & ~size_t(255);
     char* buf = nullptr;
-    MXS_CUDA(cudaMalloc(&buf, a0 + a1 + vs * (size_t)N + 256));
+    MXS_CUDA(dev_malloc(&buf, a0 + a1 + vs * (size_t)N + 256));
     int* rp = reinterpret_cast<int*>(buf);
     int* ci = reinterpret_cast<int*>(buf + a0);
     void* va = buf + a0 + a1;
@@ -431,13 +431,13 @@ spmv_status_t spmv_plan_create_ex(spmv_handle_t* h, spmv_type_t type, int R, int
         e = cudaMemcpyAsync(ci, colIdx, sizeof(int) * (size_t)N, cudaMemcpyDeviceToDevice, h->stream);
     if (e == cudaSuccess && N > 0) e = cudaMemcpyAsync(va, values, vs * (size_t)N, cudaMemcpyDeviceToDevice, h->stream);
     if (e != cudaSuccess) {
-        cudaFree(buf);
+        dev_free(buf);
         return cuda_fail(e, "plan matrix copy", __FILE__, __LINE__);
     }
     const spmv_status_t st = spmv_plan_create(h, type, R, C, N, R > 0 ? rp : nullptr, N > 0 ? ci : nullptr,
                                               N > 0 ? va : nullptr, variant, out);
     if (st != SPMV_SUCCESS) {
-        cudaFree(buf);
+        dev_free(buf);
         return st;
     }
     e = cudaStreamSynchronize(h->stream);  // the caller may free its arrays on return
@@ -485,7 +485,7 @@ static spmv_status_t plan_exec_op(spmv_handle_t* h, spmv_plan_t p, spmv_operatio
         const size_t a = (sizeof(int) * ((size_t)C + 1) + 255) & ~size_t(255);
         const size_t b = (sizeof(int) * (size_t)(N > 0 ? N : 1) + 255) & ~size_t(255);
         char* buf = nullptr;
-        MXS_CUDA(cudaMalloc(&buf, a + b + sizeof(T) * (size_t)(N > 0 ? N : 1)));
+        MXS_CUDA(dev_malloc(&buf, a + b + sizeof(T) * (size_t)(N > 0 ? N : 1)));
         int* tRp = reinterpret_cast<int*>(buf);
         int* tCi = reinterpret_cast<int*>(buf + a);
         T* tVa = reinterpret_cast<T*>(buf + a + b);
@@ -496,7 +496,7 @@ static spmv_status_t plan_exec_op(spmv_handle_t* h, spmv_plan_t p, spmv_operatio
             st = spmv_plan_create(h, p->type, C, R, N, C > 0 ? tRp : nullptr, N > 0 ? tCi : nullptr,
                                   N > 0 ? static_cast<const void*>(tVa) : nullptr, nullptr, &q);
         if (st != SPMV_SUCCESS) {
-            cudaFree(buf);
+            dev_free(buf);
             return st;
         }
         p->tPlan = q;

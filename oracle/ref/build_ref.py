@@ -1,6 +1,7 @@
 """Recipe: build the reference's own hot-path functions into
 oracle/_ref/libmuxi_ref.so, from the sources where they lie under the
-reference tree (default /root/reference, or $MUXI_REF_ROOT).
+reference tree: $MUXI_REF_ROOT, else a `reference` folder beside this
+repository's folder.  Without either the recipe is skipped.
 
 This is how the CPU oracle is pinned: tests/test_oracle_pins.py runs both on
 the same seeded inputs, and tests/golden/make_golden.py stores the
@@ -44,7 +45,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
 def ref_root() -> Path:
-    return Path(os.environ.get("MUXI_REF_ROOT", "/root/reference"))
+    env = os.environ.get("MUXI_REF_ROOT")
+    return Path(env) if env else ORACLE.parent.parent / "reference"  # beside the repository's folder
 
 
 def available() -> bool:

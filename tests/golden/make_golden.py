@@ -1,7 +1,8 @@
 """Writes the golden fixtures in this directory from the REFERENCE's own code.
 
-Run in a checkout that has the reference tree (default /root/reference, or
-$MUXI_REF_ROOT):  python tests/golden/make_golden.py
+Run where the reference tree is available ($MUXI_REF_ROOT, else a
+`reference` folder beside this repository's folder; oracle/ref/build_ref.py
+finds it the same way):  python tests/golden/make_golden.py
 
 Inputs are seeded synthetic matrices from muxi_spmv_gb300's host generators;
 every expected output comes from oracle/_ref/libmuxi_ref.so, i.e. the

@@ -54,3 +54,9 @@ def test_reference_arm_json_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
     assert line["config"]["workload"] == "poisson16k" and line["config"]["nnz"] > 0
+    # the same workload keys as the GPU arm's config (bench.workload_config), so both lines name one workload
+    import bench
+    want = bench.workload_config("poisson16k", 1, 1, 1, 1, 1, 1)
+    assert set(line["config"]) == set(want)
+    assert line["config"]["cols"] == 16384 and 0 < line["config"]["distinct_cols"] <= 16384
+    assert line["config"]["parallelism"] == "replicas1" and "pinned bit-exact" in line["cpu_baseline"]["sample"]
