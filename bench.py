@@ -526,12 +526,14 @@ def gpu_arm(args):
     e2e_val = replica_throughput(ws, nbytes, e2e_ms) / 1e9
     serial_val = replica_throughput(ws, nbytes, serial_ms) / 1e9
     pv = plan.variant.as_dict()
-    kern_names = {mx.KERNEL_MERGE: "merge_vec_kernel",
-                  mx.KERNEL_CSR5: "csr5_ordered_kernel" if pv["vectorWidth"] == 32 else "csr5_tile_kernel",
-                  mx.KERNEL_BAND: "csr5_window_kernel", mx.KERNEL_ELL: "ell_kernel",
-                  mx.KERNEL_SCALAR: "csr_rows_kernel", mx.KERNEL_VECTOR: "csr_rows_kernel"}
-    # merge-path, CSR5 and band plans launch the tile kernel and a carry fix-up
-    launches_per_step = 2 if pv["kernel"] in (mx.KERNEL_MERGE, mx.KERNEL_CSR5, mx.KERNEL_BAND) else 1
+    csr5_name = ("csr5_tile_kernel" if pv["vectorWidth"] < mx.CSR5_ORDERED else
+                 "csr5_ordered_range_kernel" if pv["threadsPerRow"] > 0 else "csr5_ordered_kernel")
+    kern_names = {mx.KERNEL_MERGE: "merge_vec_kernel", mx.KERNEL_CSR5: csr5_name,
+                  mx.KERNEL_BAND: "csr5_window_kernel", mx.KERNEL_STREAM: "csr5_stream_kernel",
+                  mx.KERNEL_ELL: "ell_kernel", mx.KERNEL_SCALAR: "csr_rows_kernel", mx.KERNEL_VECTOR: "csr_rows_kernel"}
+    # merge-path and the CSR5-tiled plans launch the tile kernel and a carry fix-up
+    launches_per_step = 2 if pv["kernel"] in (mx.KERNEL_MERGE, mx.KERNEL_CSR5, mx.KERNEL_BAND,
+                                              mx.KERNEL_STREAM) else 1
 
     traffic = None
     tf = ROOT / "profiles" / f"traffic_{args.workload}_{args.dtype}.json"

@@ -260,11 +260,23 @@ typedef enum {
     SPMV_KERNEL_CSR5 = 4,      /* sigma-nnz tiles (CSR5 metadata)           */
     SPMV_KERNEL_ELL = 5,       /* column-major ELLPACK                      */
     SPMV_KERNEL_HEURISTIC = 6, /* plan: the reference's avgNnz rule, restated */
-    SPMV_KERNEL_BAND = 7       /* ordered CSR5 tiles of 32*itemsPerThread nonzeros; each
+    SPMV_KERNEL_BAND = 7,      /* ordered CSR5 tiles of 32*itemsPerThread nonzeros; each
                                   CTA owns a range of consecutive tiles and serves the
                                   gathers that fall in a bulk-copied shared-memory
                                   window of x around its rows from there            */
+    SPMV_KERNEL_STREAM = 8     /* ordered CSR5 tiles of 32*itemsPerThread nonzeros, one
+                                  CTA per SM over a contiguous tile range; each warp's
+                                  next tiles are bulk-copied (TMA) into a ring of
+                                  threadsPerRow shared-memory slots ahead of use    */
 } spmv_kernel_t;
+
+/* CSR5 (vectorWidth field): gathers in nonzero order, and the same with the
+ * next tile's column indices and values requested before the current tile is
+ * computed (block ranges only). */
+#define SPMV_CSR5_ORDERED 32
+#define SPMV_CSR5_ORDERED_PREFETCH 64
+/* CSR5 block ranges (threadsPerRow field): one range per resident block. */
+#define SPMV_RANGE_PER_RESIDENT_BLOCK (1 << 20)
 
 /* One launch configuration of a kernel family. */
 typedef struct {
@@ -272,7 +284,10 @@ typedef struct {
     int blockSize;       /* threads per CTA: SCALAR/VECTOR 64..1024 (powers
                             of two), MERGE 128/256, CSR5 with vectorWidth
                             32 128..1024, BAND 256/512/1024 (0: 512),
-                            others 256 or 512                             */
+                            STREAM FP32 512 (ipt 16, 3 stages), 768 (ipt
+                            16, 2 stages), 1024 (ipt 8, 2 or 3 stages),
+                            STREAM FP64 512 (3) or 1024 (2) with ipt 8
+                            (0: 512), others 256 or 512                   */
     int threadsPerRow;   /* VECTOR: 1,2,4,8,16,32; CSR5 with vectorWidth 32:
                             0 = one tile per warp; n > 0 = block ranges:
                             a block of blockSize 256/384/512/640/1024
@@ -282,13 +297,18 @@ typedef struct {
                             block gives each resident block one range),
                             which its warps take one at a time; BAND: target
                             tiles per warp of a CTA's range (0: 8), fitted
-                            so the CTAs fill whole waves                  */
+                            so the CTAs fill whole waves; STREAM: shared-
+                            memory slots per warp (0: 3 at 512 threads,
+                            else 2)                                       */
     int itemsPerThread;  /* MERGE: merge items per thread (tile = block*ipt);
                             CSR5: nonzeros per lane (tile = 32*ipt);
                             BAND: 8 or 16 (0: 16 for FP32, 8 for FP64)   */
     int vectorWidth;     /* VECTOR/MERGE: 1 or 4 elements per load;
                             CSR5: 32 = gathers issued in nonzero order
-                            (32 consecutive nonzeros per instruction);
+                            (32 consecutive nonzeros per instruction), 64 =
+                            the same with the next tile's loads issued
+                            before the current tile's compute (block ranges
+                            of 512 or 1024 threads, one block per SM);
                             BAND: x window in units of 1,024 elements
                             (0: the largest the CTA shape fits)           */
 } spmv_variant_t;
@@ -504,21 +524,23 @@ SPMV_API spmv_status_t spmv_exec_f32(spmv_handle_t* handle, spmv_plan_t plan, sp
 SPMV_API spmv_status_t spmv_exec_f64(spmv_handle_t* handle, spmv_plan_t plan, spmv_operation_t op, double alpha,
                                      const double* x, double beta, double* y);
 
-/* Device-side failure word of a plan.  The BAND kernel's wait for its
- * bulk-copied x window is bounded: a wait that gives up (about 2 s) raises
- * this word (code 2), lets the copy land and returns without computing.
+/* Device-side failure word of a plan.  The BAND and STREAM kernels wait for
+ * bulk copies with a bound: a wait that gives up (about 2 s) raises this word
+ * (code 2: BAND window, code 3: STREAM tile slot), lets its copies land and
+ * returns without computing.
  * Synchronises; *code = 0 when clean, else the raised code (the call then
  * returns SPMV_ERROR_DEVICE and clears the word). */
 SPMV_API spmv_status_t spmv_plan_device_error(spmv_plan_t plan, int* code);
 
 /* Fault injection for tests (no reference counterpart; the reference has no
- * bounded waits).  enable != 0: the following executions of a BAND plan
- * initialise the window barrier with one arrival held back and wait for it at
- * most `limitCycles` SM clocks (0: 100,000), so every wait runs out; the
- * kernel then makes the held-back arrival itself, waits for its copy to land
- * and returns, and spmv_plan_device_error reports code 2.  The GPU context
- * stays usable.  enable = 0 restores normal executions.  Plans of other
- * kernels have no waits: SPMV_ERROR_UNSUPPORTED_FORMAT. */
+ * bounded waits).  enable != 0: the following executions of a BAND or STREAM
+ * plan initialise their copy barriers with one arrival held back and wait for
+ * it at most `limitCycles` SM clocks (0: 100,000), so the waits run out; the
+ * kernel then makes the held-back arrivals itself, waits for its copies to
+ * land and returns, and spmv_plan_device_error reports code 2 (BAND) or 3
+ * (STREAM).  The GPU context stays usable.  enable = 0 restores normal
+ * executions.  Plans of other kernels have no waits:
+ * SPMV_ERROR_UNSUPPORTED_FORMAT. */
 SPMV_API spmv_status_t spmv_plan_inject_wait_timeout(spmv_plan_t plan, int enable, long long limitCycles);
 
 /* Device-memory accounting and allocation-failure injection for tests (no

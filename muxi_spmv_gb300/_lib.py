@@ -27,7 +27,9 @@ SPMV_OP_NORMAL, SPMV_OP_TRANSPOSE = 0, 1
 SPMV_FORMAT_CSR, SPMV_FORMAT_COO, SPMV_FORMAT_CSR2, SPMV_FORMAT_BSR, SPMV_FORMAT_CSR5, SPMV_FORMAT_ELL = 0, 1, 2, 3, 4, 5
 
 KERNEL_AUTO, KERNEL_SCALAR, KERNEL_VECTOR, KERNEL_MERGE, KERNEL_CSR5, KERNEL_ELL, KERNEL_HEURISTIC, \
-    KERNEL_BAND = range(8)
+    KERNEL_BAND, KERNEL_STREAM = range(9)
+CSR5_ORDERED, CSR5_ORDERED_PREFETCH = 32, 64
+RANGE_PER_RESIDENT_BLOCK = 1 << 20
 
 
 class SpmvError(RuntimeError):

@@ -15,7 +15,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (GenParams, Opts, SpmvError, Variant, check, lib, KERNEL_AUTO, KERNEL_SCALAR,  # noqa: F401
-                   KERNEL_BAND,
+                   KERNEL_BAND, KERNEL_STREAM, CSR5_ORDERED, CSR5_ORDERED_PREFETCH, RANGE_PER_RESIDENT_BLOCK,
                    KERNEL_VECTOR, KERNEL_MERGE, KERNEL_CSR5, KERNEL_ELL, KERNEL_HEURISTIC,
                    SPMV_TYPE_FLOAT, SPMV_TYPE_DOUBLE, SPMV_OP_NORMAL, SPMV_OP_TRANSPOSE,
                    SPMV_FORMAT_CSR, SPMV_FORMAT_COO, SPMV_FORMAT_CSR2, SPMV_FORMAT_BSR, SPMV_FORMAT_CSR5,

@@ -199,6 +199,11 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
         __nanosleep(64);
     }
 }
+// Orders this thread's earlier generic-proxy accesses to shared memory before
+// later async-proxy (bulk-copy) writes to the same bytes.
+__device__ __forceinline__ void fence_proxy_async_shared() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 // Global -> shared bulk copy completing on `bar` (16-byte aligned, size a
 // multiple of 16).
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {

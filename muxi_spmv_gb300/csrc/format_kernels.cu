@@ -106,7 +106,11 @@ csr5_ordered_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const 
 // stays in the SM's L1) and a warp that drew short tiles takes more of them
 // (no block waits for a slow tile while others idle, as one-tile-per-warp
 // launches of large blocks do).
-template <typename T, int E, int BLOCK, int MINB>
+// PREFETCH: the next tile's column indices and values are requested before
+// the current tile's gathers and row logic (a second tile's loads held in
+// registers), so the matrix stream's memory latency overlaps this tile's work
+// instead of preceding it.
+template <typename T, int E, int BLOCK, int MINB, bool PREFETCH = false>
 __global__ void __launch_bounds__(BLOCK, MINB)
 csr5_ordered_range_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, const int* __restrict__ colIdx,
                           const T* __restrict__ values, const T* __restrict__ x, T* __restrict__ y, T alpha, T beta,
@@ -126,6 +130,24 @@ csr5_ordered_range_kernel(int numRows, int nnz, const int* __restrict__ rowPtr, 
         sEnd = min(blockIdx.x * perBlock + perBlock, (int)tiles);
     }
     __syncthreads();
+    if constexpr (PREFETCH) {
+        const int end = sEnd;
+        OrderedLoad<T, E> cur, nxt;
+        if (t < end) csr5_ordered_load<T, E>(cur, t, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
+        while (t < end) {
+            int next = 0;
+            if (lane == 0) next = atomicAdd(&sNext, 1);
+            next = __shfl_sync(0xffffffffu, next, 0);
+            if (next < end)
+                csr5_ordered_load<T, E>(nxt, next, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
+            csr5_ordered_compute<T, E, true>(cur, t, lane, nnz, rowPtr, GlobalGather<T>{x}, y, alpha, beta,
+                                             betaZero != 0, tiles, carryRow, carryVal, noEmptyRows != 0, sRpAll[w],
+                                             sPAll[w], tileBits != nullptr, betaZero == kPlainAxpby);
+            cur = nxt;
+            t = next;
+        }
+        return;
+    }
     while (t < sEnd) {
         OrderedLoad<T, E> L;
         csr5_ordered_load<T, E>(L, t, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
@@ -320,10 +342,10 @@ csr5_fixup_kernel(long long tiles, const int* __restrict__ carryRow, const T* __
 // Block-range launch: about `chunk` tiles per warp, fitted so the CTAs fill
 // whole waves of the CTAs resident at once (a chunk beyond tiles / resident
 // gives one range per resident CTA: each SM works through contiguous ranges).
-template <typename T, int E, int B, int M>
+template <typename T, int E, int B, int M, bool PF = false>
 static spmv_status_t launch_range(const int* tileRow, long long tiles, int* carryRow, T* carryVal,
                                   const RowsArgs<T>& a, int chunk, const unsigned* bits, int bzFlags, cudaStream_t s) {
-    auto kern = csr5_ordered_range_kernel<T, E, B, M>;
+    auto kern = csr5_ordered_range_kernel<T, E, B, M, PF>;
     int perSm = 0;
     MXS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, B, 0));
     const long long resident = (long long)(perSm > 0 ? perSm : 1) * current_sm_count();
@@ -338,7 +360,8 @@ static spmv_status_t launch_range(const int* tileRow, long long tiles, int* carr
 
 template <typename T, int E>
 static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* carryRow, T* carryVal,
-                                    const RowsArgs<T>& a, int block, int chunk, const unsigned* bits, cudaStream_t s) {
+                                    const RowsArgs<T>& a, int block, int chunk, const unsigned* bits, cudaStream_t s,
+                                    bool prefetch) {
     const int bzFlags = a.betaZero ? (a.alpha == T(1) ? kPlainAxpby : 1) : 0;
     if (chunk <= 0) {
         constexpr bool wide = E * sizeof(T) >= 64;  // 16 doubles or floats per lane: fewer, larger blocks
@@ -358,6 +381,13 @@ static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* ca
         }
 #undef MXS_ORDERED
         return SPMV_SUCCESS;
+    }
+    if (prefetch) {  // block ranges with the next tile's loads in flight: one block per SM
+        switch (block) {
+            case 512: return launch_range<T, E, 512, 1, true>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, bzFlags, s);
+            case 1024: return launch_range<T, E, 1024, 1, true>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, bzFlags, s);
+            default: MXS_FAIL(SPMV_ERROR_INTERNAL, "prefetching block ranges need 512 or 1024 threads (got %d)", block);
+        }
     }
     // Block ranges of about `chunk` tiles per warp.  Resident blocks per SM
     // (the register budget): 16 four-byte or 8 eight-byte values per lane
@@ -381,7 +411,7 @@ static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* ca
 template <typename T>
 spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
                        const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain, bool ordered, int block,
-                       int chunk, const Csr5Chains* chains, const unsigned* tileBits) {
+                       int chunk, const Csr5Chains* chains, const unsigned* tileBits, bool prefetch) {
     // The lane-contiguous kernel reads 16-byte quads; on arrays that are not
     // 16-byte aligned the ordered kernel (4-byte loads) runs the same tiles.
     if (!ordered && !(aligned16(a.colIdx) && aligned16(a.values))) {
@@ -391,9 +421,9 @@ spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carr
         tileBits = nullptr;
     }
     if (ordered) {
-        if (sigma == 128) MXS_TRY((launch_ordered<T, 4>(tileRow, tiles, carryRow, carryVal, a, block, chunk, tileBits, s)));
-        else if (sigma == 256) MXS_TRY((launch_ordered<T, 8>(tileRow, tiles, carryRow, carryVal, a, block, chunk, tileBits, s)));
-        else if (sigma == 512) MXS_TRY((launch_ordered<T, 16>(tileRow, tiles, carryRow, carryVal, a, block, chunk, tileBits, s)));
+        if (sigma == 128) MXS_TRY((launch_ordered<T, 4>(tileRow, tiles, carryRow, carryVal, a, block, chunk, tileBits, s, prefetch)));
+        else if (sigma == 256) MXS_TRY((launch_ordered<T, 8>(tileRow, tiles, carryRow, carryVal, a, block, chunk, tileBits, s, prefetch)));
+        else if (sigma == 512) MXS_TRY((launch_ordered<T, 16>(tileRow, tiles, carryRow, carryVal, a, block, chunk, tileBits, s, prefetch)));
         else MXS_FAIL(SPMV_ERROR_INTERNAL, "CSR5 sigma must be 128, 256 or 512 (got %d)", sigma);
     } else {
         const unsigned g = grid_for(tiles * 32, 256);
@@ -463,10 +493,10 @@ template spmv_status_t run_csr5_fixups<double>(long long, const int*, const doub
                                                cudaStream_t, cudaEvent_t, const Csr5Chains*, bool);
 template spmv_status_t run_csr5<float>(int, const int*, long long, int*, float*, const RowsArgs<float>&,
                                        cudaStream_t, cudaEvent_t, bool, int, int, const Csr5Chains*,
-                                       const unsigned*);
+                                       const unsigned*, bool);
 template spmv_status_t run_csr5<double>(int, const int*, long long, int*, double*, const RowsArgs<double>&,
                                         cudaStream_t, cudaEvent_t, bool, int, int, const Csr5Chains*,
-                                        const unsigned*);
+                                        const unsigned*, bool);
 
 // ---------------------------------------------------------------------------
 // ELL

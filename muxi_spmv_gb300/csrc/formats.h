@@ -30,7 +30,7 @@ template <typename T>
 spmv_status_t run_csr5(int sigma, const int* tileRow, long long tiles, int* carryRow, T* carryVal,
                        const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain = nullptr, bool ordered = false,
                        int block = 256, int chunk = 0, const Csr5Chains* chains = nullptr,
-                       const unsigned* tileBits = nullptr);
+                       const unsigned* tileBits = nullptr, bool prefetch = false);
 
 // The carry fix-up behind a CSR5-tiled kernel: with a chain table, one
 // thread (or warp) per chain; without one, runs of carryRow walked in tile
@@ -57,6 +57,18 @@ spmv_status_t run_band(int block, int E, int tilesPerWarp, int winK, const int* 
                        int* carryRow, T* carryVal, int* errFlag, const RowsArgs<T>& a, int numCols, cudaStream_t s,
                        cudaEvent_t afterMain, const Csr5Chains* chains, const unsigned* tileBits,
                        const BandTest& test);
+
+// Ordered CSR5 tiles fed by bulk copies into per-warp shared-memory rings of
+// `stages` tiles (stream_kernels.cu), one CTA of `block` threads per SM over
+// a contiguous tile range.  FP32: E = 16 with block 512 (3 stages) or 768 (2),
+// E = 8 with block 1024 (2 or 3); FP64: E = 8 with block 512 (3) or 1024 (2).
+// Arrays that are not 16-byte aligned run the register-prefetching block
+// ranges instead.  errFlag: raised (code 3) when a slot wait gave up.
+bool stream_shape_supported(int block, int E, int stages, bool dbl);
+template <typename T>
+spmv_status_t run_stream(int block, int E, int stages, const int* tileRow, long long tiles, int* carryRow,
+                         T* carryVal, int* errFlag, const RowsArgs<T>& a, cudaStream_t s, cudaEvent_t afterMain,
+                         const Csr5Chains* chains, const unsigned* tileBits, const BandTest& test);
 
 // Row-start masks of a CSR5 tiling for an ordered plan (matrices without
 // empty rows): sigma/32 words per tile, one cudaMalloc'd buffer in *buf.

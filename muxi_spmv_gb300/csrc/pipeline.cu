@@ -314,7 +314,8 @@ spmv_status_t spmv_pipeline_info(spmv_pipeline_t p, int* slices, int* depth, spm
         for (spmv_plan_t q : p->plans) {
             spmv_variant_t v{};
             spmv_plan_get_variant(q, &v);
-            n += (v.kernel == SPMV_KERNEL_MERGE || v.kernel == SPMV_KERNEL_CSR5 || v.kernel == SPMV_KERNEL_BAND) ? 2 : 1;
+            n += (v.kernel == SPMV_KERNEL_MERGE || v.kernel == SPMV_KERNEL_CSR5 || v.kernel == SPMV_KERNEL_BAND ||
+                  v.kernel == SPMV_KERNEL_STREAM) ? 2 : 1;
         }
         *launchesPerRequest = n;
     }

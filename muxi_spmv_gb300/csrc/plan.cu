@@ -40,13 +40,18 @@ static spmv_variant_t resolve(const spmv_variant_t* req, spmv_type_t type, int R
     if (req) v = *req;
     if (v.kernel == SPMV_KERNEL_HEURISTIC) return heuristic_variant(R, N);
     if (v.kernel == SPMV_KERNEL_AUTO) return auto_variant(type, N);
-    if (!v.blockSize) v.blockSize = v.kernel == SPMV_KERNEL_BAND ? 512 : 256;
+    if (!v.blockSize) v.blockSize = (v.kernel == SPMV_KERNEL_BAND || v.kernel == SPMV_KERNEL_STREAM) ? 512 : 256;
     if (v.kernel == SPMV_KERNEL_SCALAR) v.threadsPerRow = 1;
     if (v.kernel == SPMV_KERNEL_VECTOR && !v.threadsPerRow) v.threadsPerRow = 32;
     if (v.kernel == SPMV_KERNEL_MERGE && !v.itemsPerThread) v.itemsPerThread = v.vectorWidth == 4 ? 8 : 7;
     if (v.kernel == SPMV_KERNEL_BAND && !v.itemsPerThread) v.itemsPerThread = type == SPMV_TYPE_DOUBLE ? 8 : 16;
+    if (v.kernel == SPMV_KERNEL_STREAM) {
+        if (!v.itemsPerThread) v.itemsPerThread = (type == SPMV_TYPE_DOUBLE || v.blockSize == 1024) ? 8 : 16;
+        if (!v.threadsPerRow) v.threadsPerRow = v.blockSize == 512 ? 3 : 2;
+    }
     if (v.kernel == SPMV_KERNEL_CSR5 && !v.itemsPerThread) v.itemsPerThread = 4;  // sigma 128
-    if (!v.vectorWidth && v.kernel != SPMV_KERNEL_BAND) v.vectorWidth = 1;  // BAND: 0 = largest window
+    if (!v.vectorWidth && v.kernel != SPMV_KERNEL_BAND && v.kernel != SPMV_KERNEL_STREAM)
+        v.vectorWidth = 1;  // BAND: 0 = largest window; STREAM: unused
     return v;
 }
 
@@ -93,9 +98,14 @@ spmv_status_t plan_exec_stream(spmv_plan_t p, T alpha, const T* x, T beta, T* y,
             break;
         case SPMV_KERNEL_CSR5:
             MXS_TRY(run_csr5<T>(32 * v.itemsPerThread, p->csr5TileRow, p->csr5Tiles, p->csr5CarryRow,
-                                static_cast<T*>(p->csr5CarryVal), a, s, evEnd, v.vectorWidth == 32, v.blockSize,
-                                v.vectorWidth == 32 ? v.threadsPerRow : 0, &p->chains,
-                                static_cast<const unsigned*>(p->tileBits)));
+                                static_cast<T*>(p->csr5CarryVal), a, s, evEnd, v.vectorWidth >= 32, v.blockSize,
+                                v.vectorWidth >= 32 ? v.threadsPerRow : 0, &p->chains,
+                                static_cast<const unsigned*>(p->tileBits), v.vectorWidth == 64));
+            break;
+        case SPMV_KERNEL_STREAM:
+            MXS_TRY(run_stream<T>(v.blockSize, v.itemsPerThread, v.threadsPerRow, p->csr5TileRow, p->csr5Tiles,
+                                  p->csr5CarryRow, static_cast<T*>(p->csr5CarryVal), p->errFlag, a, s, evEnd,
+                                  &p->chains, static_cast<const unsigned*>(p->tileBits), p->bandTest));
             break;
         case SPMV_KERNEL_ELL:
             MXS_TRY(run_ell<T>(p->numRows, p->ellWidth, p->ellCol, static_cast<const T*>(p->ellVal), x, y, alpha, beta,
@@ -223,9 +233,9 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
                 }
             }
         }
-    } else if (v.kernel == SPMV_KERNEL_CSR5 || v.kernel == SPMV_KERNEL_BAND) {
+    } else if (v.kernel == SPMV_KERNEL_CSR5 || v.kernel == SPMV_KERNEL_BAND || v.kernel == SPMV_KERNEL_STREAM) {
         const int sigma = 32 * v.itemsPerThread;
-        if (v.kernel == SPMV_KERNEL_CSR5 && v.vectorWidth == 32 &&
+        if (v.kernel == SPMV_KERNEL_CSR5 && v.vectorWidth >= 32 &&
             (v.threadsPerRow > 0 ? (v.blockSize != 256 && v.blockSize != 384 && v.blockSize != 512 &&
                                     v.blockSize != 640 && v.blockSize != 1024)
                                  : (v.blockSize != 128 && v.blockSize != 256 && v.blockSize != 512 &&
@@ -239,6 +249,17 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
                     v.vectorWidth < 0)) {
             set_error(__FILE__, __LINE__, "unsupported band shape block=%d ept=%d tiles/warp=%d window=%dK",
                       v.blockSize, v.itemsPerThread, v.threadsPerRow, v.vectorWidth);
+            st = SPMV_ERROR_INTERNAL;
+        } else if (v.kernel == SPMV_KERNEL_CSR5 && v.vectorWidth >= 32 && v.vectorWidth != 32 &&
+                   (v.vectorWidth != 64 || v.threadsPerRow <= 0 || (v.blockSize != 512 && v.blockSize != 1024))) {
+            set_error(__FILE__, __LINE__,
+                      "ordered CSR5 takes vectorWidth 32, or 64 (prefetching block ranges: threadsPerRow > 0, "
+                      "512 or 1024 threads)");
+            st = SPMV_ERROR_INTERNAL;
+        } else if (v.kernel == SPMV_KERNEL_STREAM &&
+                   !stream_shape_supported(v.blockSize, v.itemsPerThread, v.threadsPerRow, type == SPMV_TYPE_DOUBLE)) {
+            set_error(__FILE__, __LINE__, "unsupported stream shape block=%d ept=%d stages=%d", v.blockSize,
+                      v.itemsPerThread, v.threadsPerRow);
             st = SPMV_ERROR_INTERNAL;
         } else if (sigma != 128 && sigma != 256 && sigma != 512) {
             set_error(__FILE__, __LINE__, "CSR5 needs itemsPerThread 4, 8 or 16 (sigma 128, 256 or 512)");
@@ -273,7 +294,7 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
                 if (st == SPMV_SUCCESS)
                     st = csr5_chains(rowPtr, R, N, sigma, p->csr5TileRow, T, &p->chainBuf, &p->chains, h->stream);
                 // ordered tiles (the CSR5 ordered kernels and the x-window kernel) take row-start masks
-                const bool ordered = v.kernel == SPMV_KERNEL_BAND || v.vectorWidth == 32;
+                const bool ordered = v.kernel != SPMV_KERNEL_CSR5 || v.vectorWidth >= 32;
                 if (st == SPMV_SUCCESS && ordered && p->noEmptyRows)
                     st = csr5_tile_bits(rowPtr, R, sigma, T, &p->tileBits, h->stream);
                 if (st == SPMV_SUCCESS) {
@@ -352,8 +373,8 @@ spmv_status_t spmv_plan_device_error(spmv_plan_t p, int* code) {
 spmv_status_t spmv_plan_inject_wait_timeout(spmv_plan_t p, int enable, long long limitCycles) {
     clear_error();
     if (!p) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "plan is NULL");
-    if (p->variant.kernel != SPMV_KERNEL_BAND)
-        MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "only BAND plans have a bounded wait to inject into");
+    if (p->variant.kernel != SPMV_KERNEL_BAND && p->variant.kernel != SPMV_KERNEL_STREAM)
+        MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "only BAND and STREAM plans have bounded waits to inject into");
     if (limitCycles < 0) MXS_FAIL(SPMV_ERROR_INVALID_MATRIX, "negative wait limit");
     p->bandTest.inject = enable != 0;
     p->bandTest.waitLimit = enable ? (limitCycles > 0 ? limitCycles : 100000) : 0;

@@ -29,10 +29,13 @@ static bool variant_applicable(const spmv_variant_t& v, int R, int N, long long 
         case SPMV_KERNEL_MERGE:
             return merge_geom_supported(merge_geom_of(v));
         case SPMV_KERNEL_CSR5:
-        case SPMV_KERNEL_BAND: {
+        case SPMV_KERNEL_BAND:
+        case SPMV_KERNEL_STREAM: {
             const int sigma = 32 * v.itemsPerThread;
             if (sigma != 128 && sigma != 256 && sigma != 512) return false;
             if (N > 0x7fffffff - 32768) return false;
+            if (v.kernel == SPMV_KERNEL_STREAM)  // the selector's space is FP32
+                return stream_shape_supported(v.blockSize, v.itemsPerThread, v.threadsPerRow, false);
             return v.kernel != SPMV_KERNEL_BAND || band_shape_supported(v.blockSize, v.itemsPerThread);
         }
         case SPMV_KERNEL_ELL:

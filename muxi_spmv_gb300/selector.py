@@ -97,10 +97,17 @@ def variant_space() -> list[Variant]:
 
 
 def variant_name(v: Variant) -> str:
-    k = {1: "scalar", 2: "vector", 3: "merge", 4: "csr5", 5: "ell", 6: "heuristic", 7: "band", 0: "auto"}
+    k = {1: "scalar", 2: "vector", 3: "merge", 4: "csr5", 5: "ell", 6: "heuristic", 7: "band", 8: "stream",
+         0: "auto"}
     name = k.get(v.kernel, str(v.kernel))
     if v.kernel == 2:
         return f"vector_b{v.blockSize}_t{v.threadsPerRow}"
+    if v.kernel == 4 and v.threadsPerRow > 0:  # CSR5 block ranges (prefetching with vectorWidth 64)
+        per = "sm" if v.threadsPerRow >= _lib.RANGE_PER_RESIDENT_BLOCK else str(v.threadsPerRow)
+        pf = "_pf" if v.vectorWidth == _lib.CSR5_ORDERED_PREFETCH else ""
+        return f"csr5r_b{v.blockSize}_e{v.itemsPerThread}_r{per}{pf}"
+    if v.kernel == 8:
+        return f"stream_b{v.blockSize}_e{v.itemsPerThread}_s{v.threadsPerRow}"
     if v.kernel in (3, 4, 7):
         return f"{name}_b{v.blockSize}_e{v.itemsPerThread}"
     return f"{name}_b{v.blockSize}"

@@ -111,7 +111,11 @@ PLAN_VARIANTS = [("band", 7, 512, 16, 0, 0), ("band", 7, 512, 8, 0, 0), ("band",
                  ("csr5o_128", 4, 256, 4, 32, 0), ("csr5o_256", 4, 256, 8, 32, 0), ("csr5o_512", 4, 256, 16, 32, 0),
                  ("csr5o_b128", 4, 128, 8, 32, 0), ("csr5o_b512", 4, 512, 8, 32, 0), ("csr5o_b1024", 4, 1024, 8, 32, 0),
                  ("csr5r_256c3", 4, 256, 8, 32, 3), ("csr5r_512c64", 4, 512, 4, 32, 64),
-                 ("csr5r_1024c8", 4, 1024, 8, 32, 8), ("csr5r_1024c1", 4, 1024, 16, 32, 1)]
+                 ("csr5r_1024c8", 4, 1024, 8, 32, 8), ("csr5r_1024c1", 4, 1024, 16, 32, 1),
+                 ("csr5r_640sm", 4, 640, 16, 32, 1 << 20), ("csr5r_384c2", 4, 384, 8, 32, 2),
+                 ("csr5pf_1024sm", 4, 1024, 8, 64, 1 << 20), ("csr5pf_512c3", 4, 512, 16, 64, 3),
+                 ("stream", 8, 512, 0, 0, 0), ("stream", 8, 1024, 8, 0, 3), ("stream", 8, 1024, 8, 0, 2),
+                 ("stream", 8, 768, 16, 0, 2)]
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
@@ -119,9 +123,14 @@ PLAN_VARIANTS = [("band", 7, 512, 16, 0, 0), ("band", 7, 512, 8, 0, 0), ("band",
 def test_plan_variants_match_oracle(mx, cuda, handle, cases, var, dtype):
     """Plan-only kernels (tile metadata built at plan creation): the x-window
     kernel (large and small windows), CSR5 at every tile size and block shape,
-    and CSR5 block ranges, on every edge case."""
+    CSR5 block ranges (plain, one per SM, prefetching) and the bulk-copy-fed
+    stream kernel, on every edge case."""
     torch = cuda
     name_, kernel, block, ept, vw, tpr = var
+    if kernel == mx.KERNEL_STREAM and dtype == np.float64 and not (ept in (0, 8) and block in (512, 1024)):
+        pytest.skip("FP64 stream shapes: 8 nonzeros per lane at 512 (3 stages) or 1024 threads (2 stages)")
+    if kernel == mx.KERNEL_STREAM and dtype == np.float64 and block == 1024:
+        tpr = 2
     for name, (rp, ci, v, cols) in cases.items():
         A = device_csr(mx, rp, ci, v.astype(dtype), cols)
         xh = mx.gen_vector(cols, 77, dtype=dtype)
@@ -158,23 +167,27 @@ def test_band_unaligned_x_reads_global(mx, cuda, handle, cases, dtype):
     p.destroy()
 
 
-def test_band_window_wait_runs_out_and_reports(mx, cuda, handle, cases):
-    """The window wait is bounded.  With one arrival of the window barrier
-    held back, every wait runs out after 100,000 clocks; the kernel makes the
-    arrival itself so its bulk copy lands, returns, and the plan reports code 2
-    (SpmvError).  The context stays usable: the next normal execution of the
-    same plan matches the oracle."""
+@pytest.mark.parametrize("kind", ["band", "stream"])
+def test_bulk_copy_wait_runs_out_and_reports(mx, cuda, handle, cases, kind):
+    """Waits on bulk copies are bounded.  With one arrival of each copy
+    barrier held back, the waits run out after 100,000 clocks; the kernel
+    makes the arrivals itself so its copies land, returns, and the plan
+    reports code 2 (BAND window) or 3 (STREAM tile slots) as SpmvError.  The
+    context stays usable: the next normal execution of the same plan matches
+    the oracle."""
     torch = cuda
     rp, ci, v, cols = cases["powerlaw60k"]
     A = device_csr(mx, rp, ci, v, cols)
     xh = mx.gen_vector(cols, 77)
     x = torch.from_numpy(xh).cuda()
-    p = mx.Plan(handle, A, mx.make_variant(mx.KERNEL_BAND, 512, 0, 16, 0))
+    var = (mx.make_variant(mx.KERNEL_BAND, 512, 0, 16, 0) if kind == "band" else
+           mx.make_variant(mx.KERNEL_STREAM, 512, 3, 16, 0))
+    p = mx.Plan(handle, A, var)
     y = torch.zeros(A.numRows, device="cuda")
     p.inject_wait_timeout(True)
     p.exec(x, y)
     torch.cuda.synchronize()
-    with pytest.raises(mx.SpmvError, match="code 2"):
+    with pytest.raises(mx.SpmvError, match="code 2" if kind == "band" else "code 3"):
         p.device_error()
     assert p.device_error() == 0  # reading the word cleared it
     p.inject_wait_timeout(False)

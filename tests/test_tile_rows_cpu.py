@@ -91,3 +91,37 @@ def test_segmented_scan_stops_at_longest_key_run():
         # and the full scan is the segmented inclusive prefix sum
         ref = np.array([vals[: l + 1][keys[: l + 1] == keys[l]].sum() for l in range(32)])
         assert np.array_equal(full, ref)
+
+
+def swizzled_word(f: int) -> int:
+    """Stored position of 16-byte word f of an FP32 product hand-off
+    (csr5_ordered.cuh: swizzled_word)."""
+    return f ^ ((f >> 3) & 7)
+
+
+@pytest.mark.parametrize("E", [4, 8, 16])
+def test_fp32_handoff_swizzle_is_conflict_free(E):
+    """FP32 tiles write product j = lane + 32e (nonzero order) into word j/4,
+    component j%4, of a swizzled layout and read a lane's E consecutive
+    products back as E/4 16-byte words.  The layout must be a permutation of
+    the 8E words, each write instruction must hit all 32 banks once, and each
+    eight-lane phase of a 16-byte read must touch eight distinct 16-byte bank
+    groups (no bank conflicts either way)."""
+    words = 8 * E
+    assert sorted(swizzled_word(f) for f in range(words)) == list(range(words))
+    for e in range(E):
+        banks = {(4 * swizzled_word((lane + 32 * e) >> 2) + ((lane + 32 * e) & 3)) % 32 for lane in range(32)}
+        assert len(banks) == 32
+    for q in range(E // 4):
+        for phase in range(4):
+            groups = {swizzled_word(lane * (E // 4) + q) % 8 for lane in range(8 * phase, 8 * phase + 8)}
+            assert len(groups) == 8
+    # lane l's words hold its products l*E .. l*E + E - 1 in order
+    store = {}
+    for lane in range(32):
+        for e in range(E):
+            j = lane + 32 * e
+            store[4 * swizzled_word(j >> 2) + (j & 3)] = j
+    for lane in range(32):
+        got = [store[4 * swizzled_word(lane * (E // 4) + q) + c] for q in range(E // 4) for c in range(4)]
+        assert got == list(range(lane * E, lane * E + E))
