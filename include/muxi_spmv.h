@@ -803,11 +803,17 @@ typedef enum {
  * nonzeros per slot of lanes (8, or 4; default 8), resident 256-thread blocks
  * per SM the kernel is compiled for (2; 3 with 4 nonzeros per slot; default
  * 2), and nonzeros per work chunk handed to a warp (a multiple of the tile,
- * which is nnzPerSlot * 32 / (k/4 rounded up to 1); default 2048). */
+ * which is nnzPerSlot * 32 / (k/4 rounded up to 1); default 2048).
+ * ordered = 1 (k = 1 only): every matrix is cut into CSR5 tiles of
+ * 32 * nnzPerSlot nonzeros (16, default, or 8) and each warp runs one tile
+ * with loads and gathers in nonzero order, as a single-matrix plan does
+ * (128-thread blocks, blocksPerSM 10 or 8 for 16 nonzeros per lane, 16 or
+ * 12 for 8; chunkNnz is ignored), joined by a per-tile carry fix-up. */
 typedef struct {
     int nnzPerSlot;
     int blocksPerSM;
     int chunkNnz;
+    int ordered;
 } spmv_batch_variant_t;
 
 /* `mats` is a host array of `count` descriptors (device pointers).  Builds

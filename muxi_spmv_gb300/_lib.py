@@ -89,7 +89,7 @@ class HostCSR(C.Structure):
 
 class BatchVariant(C.Structure):
     """spmv_batch_variant_t."""
-    _fields_ = [("nnzPerSlot", C.c_int), ("blocksPerSM", C.c_int), ("chunkNnz", C.c_int)]
+    _fields_ = [("nnzPerSlot", C.c_int), ("blocksPerSM", C.c_int), ("chunkNnz", C.c_int), ("ordered", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

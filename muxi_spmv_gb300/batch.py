@@ -124,7 +124,10 @@ def batch_variant_space(k: int) -> list[dict]:
     out = []
     for e, b in ((8, 2), (4, 2), (4, 3)):
         for c in (1024, 2048, 4096):
-            out.append({"nnzPerSlot": e, "blocksPerSM": b, "chunkNnz": c})
+            out.append({"nnzPerSlot": e, "blocksPerSM": b, "chunkNnz": c, "ordered": 0})
+    if k == 1:  # one warp per CSR5 tile, gathers in nonzero order
+        out += [{"nnzPerSlot": e, "blocksPerSM": b, "chunkNnz": 0, "ordered": 1}
+                for e, b in ((16, 10), (16, 8), (8, 16), (8, 12))]
     return out
 
 
@@ -147,10 +150,10 @@ def autotune_batch(handle: SpmvHandle, mats, k: int, xs, ys, candidates=None, re
             plan.exec(1.0, 0.0, BATCH_PERSISTENT_GRAPH)
         e1.record(s)
         e1.synchronize()
-        times[(v["nnzPerSlot"], v["blocksPerSM"], v["chunkNnz"])] = e0.elapsed_time(e1) / repeats
+        times[(v["nnzPerSlot"], v["blocksPerSM"], v["chunkNnz"], v.get("ordered", 0))] = e0.elapsed_time(e1) / repeats
         plan.destroy()
     best = min(times, key=times.get)
-    return {"nnzPerSlot": best[0], "blocksPerSM": best[1], "chunkNnz": best[2]}, times
+    return {"nnzPerSlot": best[0], "blocksPerSM": best[1], "chunkNnz": best[2], "ordered": best[3]}, times
 
 
 def _zipf_mean(s: float, K: int) -> float:

@@ -24,6 +24,7 @@
 #include "device.cuh"
 #include "kernels.h"
 #include "preprocess.h"
+#include "csr5_ordered.cuh"
 
 struct spmv_batch_s;
 
@@ -407,6 +408,49 @@ __global__ void batch_fixup_kernel(const BatchDesc* __restrict__ descs, int W, c
     for (int j = 0; j < K; ++j) y[j] += alpha * s[j];
 }
 
+// k = 1, ordered tiles: the batch's CSR5 tiles of 32*E nonzeros (each
+// matrix cut into its own tiles, concatenated) run one per warp exactly as a
+// single-matrix plan runs them (csr5_ordered.cuh: loads and gathers in
+// nonzero order, interior tiles as warp sums, row logic for the rest): no
+// slot machinery, about 48 registers, up to 40 warps per SM.  tileMat[t]
+// names the matrix of global tile t; the tile writes its carry at its
+// global index.  Tiles [tBegin, tEnd) of the batch.
+template <int E, int MINB>
+__global__ void __launch_bounds__(128, MINB)
+batch_ordered_kernel(const BatchDesc* __restrict__ descs, const int* __restrict__ tileStart,
+                     const int* __restrict__ tileMat, const int* __restrict__ tileRow, int tBegin, int tEnd,
+                     int* __restrict__ carryRow, float* __restrict__ carryVal, float alpha, float beta, int betaZero) {
+    __shared__ int sRpAll[4][kOrderedRpCap];
+    __shared__ __align__(16) float sPAll[4][ordered_slots<float, E>()];
+    const int w = threadIdx.x >> 5;
+    const long long t = tBegin + ((long long)blockIdx.x * 128 + threadIdx.x) / 32;
+    if (t >= tEnd) return;  // whole warps
+    const int m = __ldg(tileMat + t);
+    const BatchDesc d = descs[m];
+    const int ts = __ldg(tileStart + m);
+    const long long tilesM = __ldg(tileStart + m + 1) - ts;
+    csr5_ordered_tile<float, E>(t - ts, threadIdx.x & 31, d.numRows, d.nnz, d.rowPtr, d.colIdx, d.values, d.x, d.y,
+                                alpha, beta, betaZero != 0, tileRow + ts, tilesM, carryRow + ts, carryVal + ts,
+                                false, nullptr, sRpAll[w], sPAll[w], betaZero == kPlainAxpby);
+}
+
+// Adds the carries of rows split between ordered tiles: the thread at the
+// first tile of a run of tiles of one matrix carrying one row sums the run in
+// tile order (runs never cross matrices).
+__global__ void batch_ordered_fixup_kernel(const BatchDesc* __restrict__ descs, const int* __restrict__ tileMat,
+                                           int tBegin, int tEnd, const int* __restrict__ carryRow,
+                                           const float* __restrict__ carryVal, float alpha) {
+    const long long t = tBegin + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tEnd) return;
+    const int r = carryRow[t];
+    if (r < 0) return;
+    const int m = tileMat[t];
+    if (t > tBegin && carryRow[t - 1] == r && tileMat[t - 1] == m) return;
+    float sum = 0.f;
+    for (long long u = t; u < tEnd && carryRow[u] == r && tileMat[u] == m; ++u) sum += carryVal[u];
+    descs[m].y[r] += alpha * sum;
+}
+
 }  // namespace mxs
 
 using namespace mxs;
@@ -428,6 +472,7 @@ struct spmv_batch_s {
     int* dCarryRow = nullptr;
     int* dCarryMat = nullptr;
     float* dCarryVal = nullptr;
+    int* dTileMat = nullptr;  // ordered k = 1 batches: matrix of each tile
     bool vectorsSet = false;
     // graphs, keyed by the mode and the alpha/beta they were captured with
     struct G {
@@ -467,9 +512,38 @@ FixupKernel fixup_kernel_for(int k) {
     }
 }
 
+using OrderedKernel = void (*)(const BatchDesc*, const int*, const int*, const int*, int, int, int*, float*, float,
+                               float, int);
+
+OrderedKernel ordered_kernel_for(int e, int minb) {
+    if (e == 16 && minb == 10) return batch_ordered_kernel<16, 10>;
+    if (e == 16 && minb == 8) return batch_ordered_kernel<16, 8>;
+    if (e == 8 && minb == 16) return batch_ordered_kernel<8, 16>;
+    if (e == 8 && minb == 12) return batch_ordered_kernel<8, 12>;
+    return nullptr;
+}
+
+// One launch pair (tile kernel + carry fix-up) over the tiles of matrices
+// [mBegin, mEnd) of an ordered batch.
+spmv_status_t launch_ordered_range(const spmv_batch_s* b, int mBegin, int mEnd, float alpha, float beta,
+                                   cudaStream_t s) {
+    const int t0 = b->hTileStart[mBegin], t1 = b->hTileStart[mEnd];
+    if (t1 <= t0) return SPMV_SUCCESS;
+    const int bz = beta == 0.f ? (alpha == 1.f ? kPlainAxpby : 1) : 0;
+    ordered_kernel_for(b->variant.nnzPerSlot, b->variant.blocksPerSM)<<<grid_for((long long)(t1 - t0) * 32, 128), 128,
+                                                                        0, s>>>(
+        b->dDesc, b->dTileStart, b->dTileMat, b->dTileRow, t0, t1, b->dCarryRow, b->dCarryVal, alpha, beta, bz);
+    MXS_LAUNCH_CHECK();
+    batch_ordered_fixup_kernel<<<grid_for(t1 - t0, 256), 256, 0, s>>>(b->dDesc, b->dTileMat, t0, t1, b->dCarryRow,
+                                                                        b->dCarryVal, alpha);
+    MXS_LAUNCH_CHECK();
+    return SPMV_SUCCESS;
+}
+
 // One launch pair over matrices [mBegin, mEnd) with chunks of chunkTiles tiles.
 spmv_status_t launch_range(const spmv_batch_s* b, int mBegin, int mEnd, int chunkTiles, float alpha, float beta,
                            cudaStream_t s) {
+    if (b->variant.ordered) return launch_ordered_range(b, mBegin, mEnd, alpha, beta, s);
     const int tiles = b->hTileStart[mEnd] - b->hTileStart[mBegin];
     const int chunks = (tiles + chunkTiles - 1) / chunkTiles;
     const int warps = chunks < b->warps ? chunks : b->warps;
@@ -514,6 +588,7 @@ spmv_status_t spmv_batch_destroy(spmv_batch_t b) {
     dev_free(b->dTileStart);
     dev_free(b->dTileRow);
     dev_free(b->dCarryRow);
+    dev_free(b->dTileMat);
     delete b;
     return SPMV_SUCCESS;
 }
@@ -528,15 +603,28 @@ spmv_status_t spmv_batch_create_ex(spmv_handle_t* h, int count, const spmv_batch
     if (k != 1 && k != 2 && k != 4 && k != 8 && k != 16)
         MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "k must be 1, 2, 4, 8 or 16 (got %d)", k);
     spmv_batch_variant_t v = variant ? *variant : spmv_batch_variant_t{};
-    if (!v.nnzPerSlot) v.nnzPerSlot = 8;
-    if (!v.blocksPerSM) v.blocksPerSM = 2;
-    if (!v.chunkNnz) v.chunkNnz = 2048;
-    if (!batch_kernel_for(k, v.nnzPerSlot, v.blocksPerSM))
-        MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "no batch kernel for k=%d, %d nonzeros per slot, %d blocks per SM", k,
-                 v.nnzPerSlot, v.blocksPerSM);
-    const int sigma = batch_sigma(k, v.nnzPerSlot);
-    if (v.chunkNnz < sigma || v.chunkNnz % sigma)
-        MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "chunkNnz must be a positive multiple of the tile (%d)", sigma);
+    int sigma = 0;
+    if (v.ordered) {
+        if (k != 1) MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "ordered batch tiles need k = 1 (got %d)", k);
+        if (!v.nnzPerSlot) v.nnzPerSlot = 16;
+        if (!v.blocksPerSM) v.blocksPerSM = v.nnzPerSlot == 16 ? 10 : 16;
+        if (!ordered_kernel_for(v.nnzPerSlot, v.blocksPerSM))
+            MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT,
+                     "no ordered batch kernel for %d nonzeros per lane, %d blocks per SM (16: 10 or 8; 8: 16 or 12)",
+                     v.nnzPerSlot, v.blocksPerSM);
+        sigma = 32 * v.nnzPerSlot;
+        v.chunkNnz = sigma;  // one tile per warp
+    } else {
+        if (!v.nnzPerSlot) v.nnzPerSlot = 8;
+        if (!v.blocksPerSM) v.blocksPerSM = 2;
+        if (!v.chunkNnz) v.chunkNnz = 2048;
+        if (!batch_kernel_for(k, v.nnzPerSlot, v.blocksPerSM))
+            MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "no batch kernel for k=%d, %d nonzeros per slot, %d blocks per SM",
+                     k, v.nnzPerSlot, v.blocksPerSM);
+        sigma = batch_sigma(k, v.nnzPerSlot);
+        if (v.chunkNnz < sigma || v.chunkNnz % sigma)
+            MXS_FAIL(SPMV_ERROR_UNSUPPORTED_FORMAT, "chunkNnz must be a positive multiple of the tile (%d)", sigma);
+    }
     long long tiles = 0, nnzTotal = 0, maxTiles = 0;
     std::vector<int> tileStart(count + 1);
     for (int i = 0; i < count; ++i) {
@@ -576,8 +664,14 @@ spmv_status_t spmv_batch_create_ex(spmv_handle_t* h, int count, const spmv_batch
         b->hDesc[i] = BatchDesc{mats[i].rowPtr, mats[i].colIdx, mats[i].values, nullptr, nullptr, mats[i].numRows,
                                 mats[i].nnz};
     int perSM = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, batch_kernel_for(k, v.nnzPerSlot, v.blocksPerSM), 256, 0);
-    b->warps = current_sm_count() * (perSM > 0 ? perSM : 1) * 8;
+    if (v.ordered) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, ordered_kernel_for(v.nnzPerSlot, v.blocksPerSM), 128, 0);
+        b->warps = current_sm_count() * (perSM > 0 ? perSM : 1) * 4;
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, batch_kernel_for(k, v.nnzPerSlot, v.blocksPerSM), 256,
+                                                      0);
+        b->warps = current_sm_count() * (perSM > 0 ? perSM : 1) * 8;
+    }
 
     const cudaStream_t s = h->stream;
     int* tileOff = nullptr;
@@ -586,10 +680,13 @@ spmv_status_t spmv_batch_create_ex(spmv_handle_t* h, int count, const spmv_batch
     if (e == cudaSuccess) e = dev_malloc(&b->dTileStart, sizeof(int) * (count + 1));
     if (e == cudaSuccess) e = dev_malloc(&b->dTileRow, sizeof(int) * tiles);
     if (e == cudaSuccess) e = dev_malloc(&tileOff, sizeof(int) * tiles);
-    // carries: row, matrix, k values per chunk
+    // carries: row, matrix, k values per chunk (ordered: per tile, plus the
+    // matrix of each tile)
     // persistent chunks, or at most one full-GPU grid of chunks per matrix
     size_t nch = (size_t)((tiles + b->chunkTiles - 1) / b->chunkTiles);
     if (nch < (size_t)b->warps) nch = (size_t)b->warps;
+    if (v.ordered) nch = (size_t)tiles;
+    if (e == cudaSuccess && v.ordered) e = dev_malloc(&b->dTileMat, sizeof(int) * tiles);
     const size_t rowsBytes = (sizeof(int) * 2 * nch + 255) & ~size_t(255);
     const size_t cb = rowsBytes + sizeof(float) * k * nch;
     if (e == cudaSuccess) e = dev_malloc(&b->dCarryRow, cb);
@@ -604,6 +701,16 @@ spmv_status_t spmv_batch_create_ex(spmv_handle_t* h, int count, const spmv_batch
     if (e == cudaSuccess) e = cudaMemsetAsync(b->dTileRow, 0, sizeof(int) * tiles, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->dDesc, b->hDesc.data(), sizeof(BatchDesc) * count,
                                               cudaMemcpyHostToDevice, s);
+    std::vector<int> tileMat;
+    if (v.ordered) {
+        // tiles of matrices without nonzeros never write a carry: -1 (all bytes 0xff) from the start
+        if (e == cudaSuccess) e = cudaMemsetAsync(b->dCarryRow, 0xff, sizeof(int) * tiles, s);
+        tileMat.resize((size_t)tiles);
+        for (int i = 0; i < count; ++i)
+            for (int t = tileStart[i]; t < tileStart[i + 1]; ++t) tileMat[(size_t)t] = i;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(b->dTileMat, tileMat.data(), sizeof(int) * tiles, cudaMemcpyHostToDevice, s);
+    }
     if (e != cudaSuccess) st = cuda_fail(e, "batch setup", __FILE__, __LINE__);
     for (int i = 0; i < count && st == SPMV_SUCCESS; ++i)
         if (mats[i].nnz > 0)

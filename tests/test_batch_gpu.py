@@ -193,22 +193,34 @@ def test_uneven_batch_small_sample(mx, cuda, handle):
 @pytest.mark.parametrize("k,variant", [(1, {"nnzPerSlot": 4, "blocksPerSM": 3, "chunkNnz": 1024}),
                                        (2, {"nnzPerSlot": 4, "blocksPerSM": 2, "chunkNnz": 4096}),
                                        (1, {"nnzPerSlot": 8, "blocksPerSM": 2, "chunkNnz": 256}),
-                                       (16, {"nnzPerSlot": 4, "blocksPerSM": 3, "chunkNnz": 32})])
+                                       (16, {"nnzPerSlot": 4, "blocksPerSM": 3, "chunkNnz": 32}),
+                                       (1, {"nnzPerSlot": 16, "blocksPerSM": 10, "ordered": 1}),
+                                       (1, {"nnzPerSlot": 8, "blocksPerSM": 12, "ordered": 1})])
 def test_batch_variants_match_oracle(mx, cuda, handle, hbatch, dmats, k, variant):
+    """Every launch shape, including the ordered k = 1 tiles (one warp per
+    CSR5 tile, per-tile carries joined across tiles of one matrix only), on
+    the batch with empty matrices, a matrix without rows and rows over
+    thousands of tiles; alpha/beta and the plain y = A x epilogue."""
     from muxi_spmv_gb300 import batch as B
     rng = np.random.default_rng(100 + k)
     X = [rng.uniform(-1, 1, c * k).astype(np.float32) for (_, _, _, c) in hbatch]
     Y0 = [rng.uniform(-1, 1, (len(rp) - 1) * k).astype(np.float32) for (rp, _, _, _) in hbatch]
     dX = [cuda.from_numpy(x).cuda() for x in X]
     plan = B.BatchPlan(handle, dmats, k, variant)
-    assert plan.variant == variant
+    want = {"chunkNnz": 0, "ordered": 0, **variant}
+    if want["ordered"]:
+        want["chunkNnz"] = 32 * want["nnzPerSlot"]  # one tile per warp
+    assert plan.variant == want
     for mode in (B.BATCH_PERSISTENT_GRAPH, B.BATCH_LOOP):
-        dY = [cuda.from_numpy(y0.copy()).cuda() if y0.size else cuda.zeros(4, device="cuda") for y0 in Y0]
-        plan.set_vectors(dX, dY)
-        plan.exec(0.75, 0.25, mode)
-        cuda.cuda.synchronize()
-        _check(hbatch, X, Y0, [y.cpu().numpy()[:y0.size] for y, y0 in zip(dY, Y0)], k, 0.75, 0.25)
+        for alpha, beta in ((0.75, 0.25), (1.0, 0.0)):
+            dY = [cuda.from_numpy(y0.copy()).cuda() if y0.size else cuda.zeros(4, device="cuda") for y0 in Y0]
+            plan.set_vectors(dX, dY)
+            plan.exec(alpha, beta, mode)
+            cuda.cuda.synchronize()
+            _check(hbatch, X, Y0, [y.cpu().numpy()[:y0.size] for y, y0 in zip(dY, Y0)], k, alpha, beta)
     plan.destroy()
+    with pytest.raises(mx.SpmvError):
+        B.BatchPlan(handle, dmats, 2, {"ordered": 1})  # ordered tiles serve k = 1 only
     with pytest.raises(mx.SpmvError):
         B.BatchPlan(handle, dmats, 4, {"nnzPerSlot": 8, "blocksPerSM": 3})  # not built
     with pytest.raises(mx.SpmvError):
