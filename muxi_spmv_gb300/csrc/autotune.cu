@@ -39,9 +39,14 @@ static const spmv_variant_t kSpace[] = {
     {SPMV_KERNEL_CSR5, 128, 0, 16, 32},
     {SPMV_KERNEL_CSR5, 512, 0, 8, 32},
     {SPMV_KERNEL_BAND, 512, 0, 16, 0},
-    {SPMV_KERNEL_BAND, 512, 0, 8, 0},
-    {SPMV_KERNEL_BAND, 1024, 0, 16, 0},
     {SPMV_KERNEL_ELL, 256, 0, 0, 1},
+    // block ranges, one per resident block (contiguous tiles per SM)
+    {SPMV_KERNEL_CSR5, 1024, SPMV_RANGE_PER_RESIDENT_BLOCK, 16, SPMV_CSR5_ORDERED},
+    {SPMV_KERNEL_CSR5, 640, SPMV_RANGE_PER_RESIDENT_BLOCK, 16, SPMV_CSR5_ORDERED},
+    // the same with the next tile's loads in flight during the current tile
+    {SPMV_KERNEL_CSR5, 1024, SPMV_RANGE_PER_RESIDENT_BLOCK, 8, SPMV_CSR5_ORDERED_PREFETCH},
+    {SPMV_KERNEL_CSR5, 512, SPMV_RANGE_PER_RESIDENT_BLOCK, 16, SPMV_CSR5_ORDERED_PREFETCH},
+    {SPMV_KERNEL_STREAM, 1024, 2, 8, 0},
 };
 constexpr int kSpaceSize = (int)(sizeof(kSpace) / sizeof(kSpace[0]));
 

@@ -300,7 +300,7 @@ def test_autotune_reports_every_variant(mx, sel, cuda, handle, name):
     rp, ci, v, A = _small(mx, name)
     space = sel.variant_space()
     ms, best = sel.autotune(handle, A, None, repeats=0)
-    assert len(ms) == len(space) == 25
+    assert len(ms) == len(space) == 28
     ok = ms > 0
     assert best == int(np.where(ok, ms, np.inf).argmin())
     maxlen = int(np.diff(rp).max())
