@@ -9,7 +9,8 @@ lengths, Zipf lengths (s in [1.3, 2.5]), banded (width 3..1025) and
 block-diagonal (8..256 blocks) -- with rows log-uniform in [1e4, 1e7] and mean
 row length log-uniform in [2, 128], FP32 N(0,1) values; seeds from
 STENCIL_SEED0 on are grid stencils (2D 5-point, 3D 27-point), from
-POWERLAW_SEED0 on power-law rows with a near-diagonal share.  Each matrix gets its
+POWERLAW_SEED0 on power-law rows with a near-diagonal share (from
+LARGE_POWERLAW_SEED0 on with 2e6..1e7 rows).  Each matrix gets its
 32 features (spmv_matrix_features) and the exhaustive autotuner's time for
 every variant of the space plus the reference heuristic's pick.  Records are
 written in chunks, so an interrupted run resumes where it stopped.
@@ -46,6 +47,7 @@ LAWS = ("poisson", "zipf", "banded", "blockdiag", "stencil", "powerlaw")
 # LAWS[seed % 4].
 STENCIL_SEED0 = 1_000_000
 POWERLAW_SEED0 = 2_000_000
+LARGE_POWERLAW_SEED0 = 2_000_250  # after the 250 power-law seeds of up to 2e6 rows
 HEURISTIC_COL = -1  # last column of the label matrix: the heuristic's variant
 DEFAULT_VARIANT = Variant(api.KERNEL_CSR5, 128, 0, 16, 32)  # the FP32 AUTO plan without a model
 
@@ -112,9 +114,14 @@ def stencil_spec(rng, seed: int, max_rows: int):
 def powerlaw_spec(rng, seed: int, max_rows: int):
     """Zipf(s) row lengths, s in [1.5, 2.2], clipped at 256..65,536; a share
     p in [0.3, 0.95] of the columns within +-band (band 64..8,192) of the
-    diagonal, the rest uniform; rows log-uniform 1e4..min(max_rows, 2e6)."""
+    diagonal, the rest uniform; rows log-uniform 1e4..min(max_rows, 2e6), and
+    from LARGE_POWERLAW_SEED0 on log-uniform 2e6..min(max_rows, 1e7) (the
+    benchmark's 8.4M-row scale, where other kernels win than at 2e6 rows)."""
     gseed = 1_000_003 * seed + 17
-    R = int(round(10 ** rng.uniform(4, math.log10(min(max_rows, 2_000_000)))))
+    if seed >= LARGE_POWERLAW_SEED0:
+        R = int(round(10 ** rng.uniform(math.log10(2_000_000), math.log10(min(max_rows, 10_000_000)))))
+    else:
+        R = int(round(10 ** rng.uniform(4, math.log10(min(max_rows, 2_000_000)))))
     s = float(rng.uniform(1.5, 2.2))
     clip = int(2 ** rng.integers(8, 17))
     band = int(round(2 ** rng.uniform(6, 13)))
