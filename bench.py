@@ -333,7 +333,7 @@ def gpu_arm(args):
         from muxi_spmv_gb300 import selector as S
         model = S.MLP.load(S.DEFAULT_MODEL)
         # AUTO plans take the learned pick; with the fallback, the variants
-        # predicted within 2% of it are timed at plan creation and the fastest kept
+        # predicted within 5% of it are timed at plan creation and the fastest kept
         S.set_selector(h, model, S.SELECT_LEARNED_FALLBACK if args.select == "learned_fallback" else S.SELECT_LEARNED)
     perm = None
     if args.colperm != "none":
@@ -880,9 +880,9 @@ def main():
     ap.add_argument("--no-vendor", action="store_true", help="skip the cuSPARSE comparison")
     ap.add_argument("--no-subrecords", action="store_true",
                     help="skip the other configurations and the selector record (profiling runs)")
-    ap.add_argument("--select", default="default", choices=["default", "learned", "learned_fallback"],
+    ap.add_argument("--select", default="learned_fallback", choices=["default", "learned", "learned_fallback"],
                     help="AUTO plan: the fixed default variant, the learned selector's pick, or that pick with the "
-                         "variants predicted within 2%% of it timed at plan creation")
+                         "variants predicted within 5%% of it timed at plan creation")
     ap.add_argument("--slices", type=int, default=1, help="host pipeline row slices")
     ap.add_argument("--depth", type=int, default=2, help="host pipeline requests in flight")
     ap.add_argument("--scale-rows", type=int, default=0, help="same law on this many rows (profiling cases)")

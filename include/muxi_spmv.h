@@ -749,7 +749,7 @@ typedef enum {
     SPMV_SELECT_AUTOTUNE = 2,      /* time the whole space                      */
     SPMV_SELECT_LEARNED_TOPK = 3,  /* time only the model's topK best guesses   */
     SPMV_SELECT_LEARNED_FALLBACK = 4 /* learned pick; when other variants are
-                                        predicted within 2% of it (low
+                                        predicted within 5% of it (low
                                         confidence), time those too (at most
                                         topK, default 3) and take the fastest */
 } spmv_select_mode_t;
@@ -770,7 +770,7 @@ SPMV_API spmv_status_t spmv_set_selector(spmv_handle_t* handle, spmv_mlp_t model
 /* How AUTO plans on this handle use the registered model:
  * SPMV_SELECT_LEARNED (default: the model's pick, about 0.15 ms) or
  * SPMV_SELECT_LEARNED_FALLBACK (plan creation also times the variants
- * predicted within 2% of the pick). */
+ * predicted within 5% of the pick). */
 SPMV_API spmv_status_t spmv_set_selector_mode(spmv_handle_t* handle, spmv_select_mode_t mode);
 
 /* ------------------------------------------------------------------ */

@@ -46,8 +46,8 @@ static bool variant_applicable(const spmv_variant_t& v, int R, int N, long long 
 }
 
 // Predicted log-time gap under which the learned pick counts as uncertain
-// (SPMV_SELECT_LEARNED_FALLBACK): 0.02, about 2%.
-constexpr float kFallbackMargin = 0.02f;
+// (SPMV_SELECT_LEARNED_FALLBACK): 0.05, about 5%.
+constexpr float kFallbackMargin = 0.05f;
 
 static bool same_variant(const spmv_variant_t& a, const spmv_variant_t& b) {
     return a.kernel == b.kernel && a.blockSize == b.blockSize && a.threadsPerRow == b.threadsPerRow &&

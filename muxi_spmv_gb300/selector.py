@@ -231,7 +231,7 @@ def select(handle: SpmvHandle, A, mode: int = SELECT_LEARNED, model: MLP | None 
 
 def set_selector(handle: SpmvHandle, model: MLP | None, mode: int = SELECT_LEARNED):
     """Makes AUTO plans on `handle` use `model` (None clears it); mode
-    SELECT_LEARNED_FALLBACK also times the variants predicted within 2%."""
+    SELECT_LEARNED_FALLBACK also times the variants predicted within 5%."""
     check(lib().spmv_set_selector(handle.raw, model.raw if model is not None else None), "spmv_set_selector")
     check(lib().spmv_set_selector_mode(handle.raw, mode), "spmv_set_selector_mode")
 
