@@ -408,3 +408,37 @@ def test_committed_model_on_held_out_corpus_gpu(sel, cuda):
     assert rep["learned_regret"]["mean"] <= 0.05
     assert rep["learned_regret"]["mean"] < rep["heuristic_regret"]["mean"]
     assert rep["learned_regret"]["mean"] < rep["default_csr5_regret"]["mean"]
+
+
+@pytest.mark.skipif(not DEFAULT_MODEL.exists(), reason="no trained selector model committed")
+def test_learned_selection_is_100x_cheaper_than_autotune(mx, sel, cuda, handle):
+    """The selection-cost claim, re-measured: on three corpus matrices of
+    different laws (banded rows, a grid stencil, power-law rows), the learned
+    pick (features + MLP forward + rank, median of 10 warm calls) costs at
+    least 100x less wall time than spmv_select(AUTOTUNE), which times every
+    applicable variant of the space as a plan."""
+    import time
+    from muxi_spmv_gb300 import selector_train as st
+    model = sel.MLP.load(DEFAULT_MODEL)
+    ratios = []
+    for seed in (6, 1_000_002, 2_000_003):  # banded, stencil, power law
+        spec, law, _ = st.spec_for_seed(seed, max_rows=1_000_000)
+        if law == "powerlaw":
+            rp, ci, v = mx.generate(spec)
+            A = mx.CSRMatrix(rp, ci, v, spec.numCols).copyToDevice()
+        else:
+            A = sel.gen_device(spec)
+        cuda.cuda.synchronize()
+        sel.select(handle, A, sel.SELECT_LEARNED, model)  # warm
+        t = []
+        for _ in range(10):
+            cuda.cuda.synchronize()
+            t0 = time.perf_counter()
+            sel.select(handle, A, sel.SELECT_LEARNED, model)
+            cuda.cuda.synchronize()
+            t.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        sel.select(handle, A, sel.SELECT_AUTOTUNE)
+        cuda.cuda.synchronize()
+        ratios.append((time.perf_counter() - t0) / float(np.median(t)))
+    assert min(ratios) >= 100.0, ratios
