@@ -308,7 +308,7 @@ typedef struct {
                             (32 consecutive nonzeros per instruction), 64 =
                             the same with the next tile's loads issued
                             before the current tile's compute (block ranges
-                            of 512 or 1024 threads, one block per SM);
+                            of 512, 768 or 1024 threads);
                             BAND: x window in units of 1,024 elements
                             (0: the largest the CTA shape fits)           */
 } spmv_variant_t;

@@ -382,11 +382,15 @@ static spmv_status_t launch_ordered(const int* tileRow, long long tiles, int* ca
 #undef MXS_ORDERED
         return SPMV_SUCCESS;
     }
-    if (prefetch) {  // block ranges with the next tile's loads in flight: one block per SM
+    if (prefetch) {  // block ranges with the next tile's loads in flight (two tiles' loads in registers)
+        constexpr bool small = E * sizeof(T) <= 32;  // 8 four-byte values per lane: two 512-thread blocks fit
         switch (block) {
-            case 512: return launch_range<T, E, 512, 1, true>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, bzFlags, s);
+            case 512:
+                if constexpr (small) return launch_range<T, E, 512, 2, true>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, bzFlags, s);
+                else return launch_range<T, E, 512, 1, true>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, bzFlags, s);
+            case 768: return launch_range<T, E, 768, 1, true>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, bzFlags, s);
             case 1024: return launch_range<T, E, 1024, 1, true>(tileRow, tiles, carryRow, carryVal, a, chunk, bits, bzFlags, s);
-            default: MXS_FAIL(SPMV_ERROR_INTERNAL, "prefetching block ranges need 512 or 1024 threads (got %d)", block);
+            default: MXS_FAIL(SPMV_ERROR_INTERNAL, "prefetching block ranges need 512, 768 or 1024 threads (got %d)", block);
         }
     }
     // Block ranges of about `chunk` tiles per warp.  Resident blocks per SM

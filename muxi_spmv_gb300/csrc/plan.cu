@@ -235,7 +235,7 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
         }
     } else if (v.kernel == SPMV_KERNEL_CSR5 || v.kernel == SPMV_KERNEL_BAND || v.kernel == SPMV_KERNEL_STREAM) {
         const int sigma = 32 * v.itemsPerThread;
-        if (v.kernel == SPMV_KERNEL_CSR5 && v.vectorWidth >= 32 &&
+        if (v.kernel == SPMV_KERNEL_CSR5 && v.vectorWidth == 32 &&
             (v.threadsPerRow > 0 ? (v.blockSize != 256 && v.blockSize != 384 && v.blockSize != 512 &&
                                     v.blockSize != 640 && v.blockSize != 1024)
                                  : (v.blockSize != 128 && v.blockSize != 256 && v.blockSize != 512 &&
@@ -251,10 +251,11 @@ spmv_status_t spmv_plan_create(spmv_handle_t* h, spmv_type_t type, int R, int C,
                       v.blockSize, v.itemsPerThread, v.threadsPerRow, v.vectorWidth);
             st = SPMV_ERROR_INTERNAL;
         } else if (v.kernel == SPMV_KERNEL_CSR5 && v.vectorWidth >= 32 && v.vectorWidth != 32 &&
-                   (v.vectorWidth != 64 || v.threadsPerRow <= 0 || (v.blockSize != 512 && v.blockSize != 1024))) {
+                   (v.vectorWidth != 64 || v.threadsPerRow <= 0 ||
+                    (v.blockSize != 512 && v.blockSize != 768 && v.blockSize != 1024))) {
             set_error(__FILE__, __LINE__,
                       "ordered CSR5 takes vectorWidth 32, or 64 (prefetching block ranges: threadsPerRow > 0, "
-                      "512 or 1024 threads)");
+                      "512, 768 or 1024 threads)");
             st = SPMV_ERROR_INTERNAL;
         } else if (v.kernel == SPMV_KERNEL_STREAM &&
                    !stream_shape_supported(v.blockSize, v.itemsPerThread, v.threadsPerRow, type == SPMV_TYPE_DOUBLE)) {
