@@ -8,7 +8,8 @@ corpus: seeded matrices generated on the GPU, one law per seed -- Poisson row
 lengths, Zipf lengths (s in [1.3, 2.5]), banded (width 3..1025) and
 block-diagonal (8..256 blocks) -- with rows log-uniform in [1e4, 1e7] and mean
 row length log-uniform in [2, 128], FP32 N(0,1) values; seeds from
-STENCIL_SEED0 on are grid stencils (2D 5-point, 3D 27-point), from
+STENCIL_SEED0 on are grid stencils (2D 5-point, 3D 27-point; from
+LARGE_STENCIL_SEED0 on at the benchmark's 1e7-row scale), from
 POWERLAW_SEED0 on power-law rows with a near-diagonal share (from
 LARGE_POWERLAW_SEED0 on with 2e6..1e7 rows).  Each matrix gets its
 32 features (spmv_matrix_features) and the exhaustive autotuner's time for
@@ -46,6 +47,7 @@ LAWS = ("poisson", "zipf", "banded", "blockdiag", "stencil", "powerlaw")
 # benchmark's law, generated on the host); below both the law is
 # LAWS[seed % 4].
 STENCIL_SEED0 = 1_000_000
+LARGE_STENCIL_SEED0 = 1_000_500  # after the 500 stencil seeds of the first range
 POWERLAW_SEED0 = 2_000_000
 LARGE_POWERLAW_SEED0 = 2_000_250  # after the 250 power-law seeds of up to 2e6 rows
 HEURISTIC_COL = -1  # last column of the label matrix: the heuristic's variant
@@ -94,16 +96,21 @@ def spec_for_seed(seed: int, max_rows: int = 10_000_000, max_nnz: int = 600_000_
 
 def stencil_spec(rng, seed: int, max_rows: int):
     """A 2D 5-point grid (rows log-uniform 1e4..max_rows, aspect 1..16) or a
-    3D 27-point grid (rows log-uniform 1e4..max_rows/4)."""
+    3D 27-point grid (rows log-uniform 1e4..max_rows/4); from
+    LARGE_STENCIL_SEED0 on, 2D grids of 1e7..2e7 rows and 3D grids of
+    2.5e6..1.7e7 rows (the benchmark's 16.8M-row stencils)."""
     gseed = 1_000_003 * seed + 17
+    large = seed >= LARGE_STENCIL_SEED0
+    lo2, hi2 = (7.0, math.log10(2e7)) if large else (4.0, math.log10(max_rows))
+    lo3, hi3 = (math.log10(2.5e6), math.log10(1.7e7)) if large else (4.0, math.log10(max_rows / 4))
     if rng.uniform() < 0.5:
-        R = 10 ** rng.uniform(4, math.log10(max_rows))
+        R = 10 ** rng.uniform(lo2, hi2)
         aspect = 2 ** rng.uniform(0, 4)
         ny = max(2, int(round(math.sqrt(R * aspect))))
         nx = max(2, int(round(R / ny)))
         spec = GenSpec(GEN_STENCIL2D, nx * ny, nx * ny, float(nx), float(ny), 0.0, 0.0, gseed)
         return spec, "stencil", 5.0
-    R = 10 ** rng.uniform(4, math.log10(max_rows / 4))
+    R = 10 ** rng.uniform(lo3, hi3)
     dims = [max(2, int(round(R ** (1 / 3) * 2 ** rng.uniform(-0.5, 0.5)))) for _ in range(2)]
     n0 = max(2, int(round(R / (dims[0] * dims[1]))))
     n = n0 * dims[0] * dims[1]
