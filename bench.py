@@ -281,25 +281,35 @@ def selector_record(args, mx, h, A, x, y, stream, dev):
     torch.cuda.synchronize(dev)
     learned_s = (time.perf_counter() - t) / reps
     t = time.perf_counter()
+    fb, fi = S.select(h, A, S.SELECT_LEARNED_FALLBACK, model)
+    torch.cuda.synchronize(dev)
+    fallback_s = time.perf_counter() - t
+    t = time.perf_counter()
     best, bi = S.select(h, A, S.SELECT_AUTOTUNE)
     torch.cuda.synchronize(dev)
     autotune_s = time.perf_counter() - t
     times = {}
-    for tag, var in (("learned", learned), ("autotune", best)):
+    for tag, var in (("learned", learned), ("fallback", fb), ("autotune", best)):
         p = mx.Plan(h, A, var)
         step_ms, _ = time_plan(torch, p, x, y, stream, dev, args.steps, args.warmup)
         times[tag] = step_ms
         p.destroy()
     model.destroy()
     return {"matrix": args.workload, "learned_pick": S.variant_name(space[li]) if li >= 0 else str(learned),
+            "fallback_pick": S.variant_name(space[fi]) if fi >= 0 else str(fb),
             "autotune_pick": S.variant_name(space[bi]) if bi >= 0 else str(best),
-            "learned_ms": round(times["learned"], 5), "autotune_ms": round(times["autotune"], 5),
+            "learned_ms": round(times["learned"], 5), "fallback_ms": round(times["fallback"], 5),
+            "autotune_ms": round(times["autotune"], 5),
             "regret": round(times["learned"] / times["autotune"] - 1.0, 4),
-            "selection_ms": {"learned": round(learned_s * 1e3, 3), "autotune": round(autotune_s * 1e3, 3)},
+            "fallback_regret": round(times["fallback"] / times["autotune"] - 1.0, 4),
+            "selection_ms": {"learned": round(learned_s * 1e3, 3), "fallback": round(fallback_s * 1e3, 3),
+                             "autotune": round(autotune_s * 1e3, 3)},
             "cost_ratio": round(autotune_s / max(learned_s, 1e-9), 1),
-            "note": "selection = spmv_select (features + MLP forward + rank) vs spmv_select(AUTOTUNE) "
-                    "(every applicable variant timed as a plan); regret from both picks' plans timed "
-                    "back to back with CUDA events"}
+            "fallback_cost_ratio": round(autotune_s / max(fallback_s, 1e-9), 1),
+            "note": "selection = spmv_select (features + MLP forward + rank), the same with the variants "
+                    "predicted within 5% timed (the mode of the benchmark's AUTO plans), and "
+                    "spmv_select(AUTOTUNE) (every applicable variant timed as a plan); regrets from the picks' "
+                    "plans timed back to back with CUDA events"}
 
 
 def gpu_arm(args):
