@@ -193,8 +193,8 @@ def cpu_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
-SUB_WORKLOADS = (("powerlaw8m", "f64"), ("powerlaw8m_c1024", "f32"), ("stencil2d_4096", "f32"),
-                 ("stencil3d_256", "f32"))
+SUB_WORKLOADS = (("poisson16k", "f32"), ("powerlaw8m", "f64"), ("powerlaw8m_c1024", "f32"),
+                 ("stencil2d_4096", "f32"), ("stencil3d_256", "f32"))
 
 
 def time_plan(torch, plan, x, y, stream, dev, steps, warmup):
@@ -223,8 +223,45 @@ def time_plan(torch, plan, x, y, stream, dev, steps, warmup):
     return step_ms, km / max(kl, 1)
 
 
+def l2_resident_record(torch, plan, x, y, stream, dev, nbytes, l2_bytes):
+    """Matrices that fit in L2 (the 16K Poisson case): SpMVs replayed from a
+    CUDA graph, warm (matrix and x in L2) and with L2 flushed before each
+    SpMV (a buffer twice the L2 written, its own time subtracted).  None when
+    the matrix and vectors take more than half the L2."""
+    if nbytes * 2 >= l2_bytes:
+        return None
+    reps, inner = 10, 20
+    flush = torch.empty(2 * l2_bytes // 4, dtype=torch.float32, device=dev)
+
+    def graph_ms(body):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            for _ in range(inner):
+                body()
+        g.replay()
+        torch.cuda.synchronize(dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            g.replay()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        return a.elapsed_time(b) / (reps * inner)
+
+    with torch.cuda.stream(stream):
+        warm = graph_ms(lambda: plan.exec(x, y))
+        both = graph_ms(lambda: (flush.fill_(1.0), plan.exec(x, y)))
+        fl = graph_ms(lambda: flush.fill_(1.0))
+    del flush
+    return {"graph_warm": {"value": round(nbytes / (warm * 1e-3) / 1e9, 3), "us_per_spmv": round(warm * 1e3, 3)},
+            "graph_l2_flushed": {"value": round(nbytes / (max(both - fl, 1e-6) * 1e-3) / 1e9, 3),
+                                 "us_per_spmv": round((both - fl) * 1e3, 3)},
+            "note": f"matrix + vectors {int(nbytes)} B fit the {l2_bytes} B L2; {reps}x{inner} SpMVs per figure "
+                    "from one CUDA graph; flushed = (flush + SpMV) - flush, flush = writing twice the L2"}
+
+
 def sub_record(args, mx, W, oracle, h, stream, dev, name, dt, peak):
-    """One compact record of another BASELINE configuration: full-size
+    """One compact record of another benchmark configuration: full-size
     matrix, the AUTO plan, full-size parity against the FP64 oracle, step
     and kernel GB/s with the clocks sampled during the timed region."""
     import torch
@@ -255,7 +292,13 @@ def sub_record(args, mx, W, oracle, h, stream, dev, name, dt, peak):
            "frac": round(nbytes / (kern_ms * 1e-3) / 1e9 / peak, 4),
            "parity": {"rows_checked": int(A.numRows), "max_err_over_bound": float(r.max()),
                       "rows_out_of_bound": int((r > 1).sum())},
-           "clocks": clocks.summary(), "generate_s": round(gen_s, 2)}
+           "clocks": clocks.summary(), "generate_s": round(gen_s, 2),
+           "l2": ("inputs larger than L2 (no flush)" if nbytes * 2 >= int(h.l2CacheBytes) else
+                  "fits in L2: value and kernel figures warm; l2_resident.graph_l2_flushed has L2 flushed "
+                  "before each SpMV")}
+    l2res = l2_resident_record(torch, plan, x, y, stream, dev, nbytes, int(h.l2CacheBytes))
+    if l2res is not None:
+        rec["l2_resident"] = l2res
     if rec["parity"]["rows_out_of_bound"]:
         print(f"PARITY FAILURE {name} {dt}: {rec['parity']}", file=sys.stderr)
     plan.destroy()
@@ -464,40 +507,8 @@ def gpu_arm(args):
         if pipe_parity["rows_out_of_bound"]:
             print(f"PIPELINE PARITY FAILURE: {pipe_parity}", file=sys.stderr)
         pipe.destroy()
-    # ---- matrices that fit in L2 (the 16K Poisson case): SpMVs replayed from a
-    # CUDA graph, warm (matrix and x in L2) and with L2 flushed before each
-    # SpMV (a buffer twice the L2 written, its own time subtracted).
-    l2res = None
-    l2_bytes = int(h.l2CacheBytes)
-    if nbytes * 2 < l2_bytes:
-        reps, inner = 10, 20
-        flush = torch.empty(2 * l2_bytes // 4, dtype=torch.float32, device=dev)
-
-        def graph_ms(body):
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g, stream=stream):
-                for _ in range(inner):
-                    body()
-            g.replay()
-            torch.cuda.synchronize(dev)
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            for _ in range(reps):
-                g.replay()
-            b.record(stream)
-            torch.cuda.synchronize(dev)
-            return a.elapsed_time(b) / (reps * inner)
-
-        with torch.cuda.stream(stream):
-            warm = graph_ms(lambda: plan.exec(x, y))
-            both = graph_ms(lambda: (flush.fill_(1.0), plan.exec(x, y)))
-            fl = graph_ms(lambda: flush.fill_(1.0))
-        l2res = {"graph_warm": {"value": round(nbytes / (warm * 1e-3) / 1e9, 3), "us_per_spmv": round(warm * 1e3, 3)},
-                 "graph_l2_flushed": {"value": round(nbytes / (max(both - fl, 1e-6) * 1e-3) / 1e9, 3),
-                                      "us_per_spmv": round((both - fl) * 1e3, 3)},
-                 "note": f"matrix + vectors {int(nbytes)} B fit the {l2_bytes} B L2; {reps}x{inner} SpMVs per figure "
-                         "from one CUDA graph; flushed = (flush + SpMV) - flush, flush = writing twice the L2"}
-        del flush
+    # ---- matrices that fit in L2 (the 16K Poisson case): graph replays
+    l2res = l2_resident_record(torch, plan, x, y, stream, dev, nbytes, int(h.l2CacheBytes))
 
     # ---- the vendor library on the same matrix and x: cuSPARSE SpMV through
     # torch.sparse (context only; nothing of ours on this path).
@@ -611,6 +622,7 @@ def gpu_arm(args):
         torch.cuda.empty_cache()
         line["subrecords"] = [sub_record(args, mx, W, oracle, h, stream, dev, name, dt, peak)
                               for name, dt in SUB_WORKLOADS if (name, dt) != (args.workload, args.dtype)]
+        line["subrecords"].append(batch_subrecord(args, mx, oracle, stream, dev, peak, peak_kind))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if plan is not None:
@@ -618,6 +630,277 @@ def gpu_arm(args):
     h.destroy()
     if ws > 1:
         dist.destroy_process_group()
+
+
+def batch_subrecord(args, mx, oracle, stream, dev, peak, peak_kind):
+    """The uneven batch at k=1 (1,024 matrices) as one compact record: the
+    persistent launch from a CUDA graph against the two per-matrix loops,
+    on a handle of its own (default AUTO plans in the loop, as a user of
+    the reference's entry points would make them)."""
+    import torch
+    from muxi_spmv_gb300 import batch as B
+    from muxi_spmv_gb300 import selector as S
+    h = mx.spmv_create_handle()
+    h.set_stream(stream)
+    t0 = time.time()
+    mats = [S.gen_device(s.spec) for s in B.uneven_specs(args.batch_count, seed=0)]
+    torch.cuda.synchronize(dev)
+    gen_s = time.time() - t0
+    distinct = [mx.count_distinct_columns(A, stream) for A in mats]
+    ctx = dict(mx=mx, B=B, oracle=oracle, h=h, stream=stream, dev=dev, mats=mats, distinct=distinct, rank=0, ws=1,
+               local=dev.index or 0, peak=peak, peak_kind=peak_kind, gen_s=gen_s,
+               sumR=sum(A.numRows for A in mats), sumC=sum(A.numCols for A in mats), sumN=sum(A.nnz for A in mats))
+    rec = batch_k_line(args, ctx, "1", compact=True)
+    del mats, ctx
+    torch.cuda.empty_cache()
+    h.destroy()
+    return rec
+
+
+def batch_k_line(args, ctx, kspec, compact=False):
+    """One k of the uneven batch: the JSON line of that k (see batched_arm).
+    compact: the persistent graph and the two per-matrix loops only (no
+    e2e, no CPU sample), for the record inside the default benchmark line."""
+    import torch
+    mx, B, oracle, h, stream, dev = (ctx[k] for k in ("mx", "B", "oracle", "h", "stream", "dev"))
+    mats, distinct, rank, ws, local = (ctx[k] for k in ("mats", "distinct", "rank", "ws", "local"))
+    peak, peak_kind, gen_s, sumR, sumC, sumN = (ctx[k] for k in ("peak", "peak_kind", "gen_s", "sumR", "sumC",
+                                                                   "sumN"))
+    L = mx.lib()
+
+    def aligned_slices(sizes):
+        offs, o = [], 0
+        for n in sizes:
+            offs.append(o)
+            o += (n + 3) // 4 * 4
+        return offs, max(o, 4)
+
+    # "mixed": each matrix draws its own k from {1, 2, 4, 8, 16} (seeded);
+    # the batch runs as a group of single-k batches in one graph
+    mixed = kspec == "mixed"
+    if mixed:
+        kk = [int(z) for z in np.random.default_rng(4242 + rank).choice([1, 2, 4, 8, 16], len(mats))]
+        k = "mixed"
+    else:
+        k = int(kspec)
+        kk = [k] * len(mats)
+    xo, xn = aligned_slices([A.numCols * ki for A, ki in zip(mats, kk)])
+    yo, yn = aligned_slices([A.numRows * ki for A, ki in zip(mats, kk)])
+    Xd = torch.empty(xn, dtype=torch.float32, device=dev)
+    Yd = torch.empty(yn, dtype=torch.float32, device=dev)
+    mx.check(L.spmv_gen_device_vector_f32(xn, 1000 + (0 if mixed else k), -1.0, 1.0, Xd.data_ptr(), None),
+             "gen x")
+    xs = [Xd[o:o + A.numCols * ki] for o, A, ki in zip(xo, mats, kk)]
+    ys = [Yd[o:o + max(A.numRows * ki, 1)] for o, A, ki in zip(yo, mats, kk)]
+    # launch shape picked by the batch autotuner on this batch (per k group)
+    if mixed:
+        best_v, tune_ms = {}, {}
+        for kg in sorted(set(kk)):
+            sel_ = [i for i, ki in enumerate(kk) if ki == kg]
+            bv, tm = B.autotune_batch(h, [mats[i] for i in sel_], kg, [xs[i] for i in sel_],
+                                      [ys[i] for i in sel_], repeats=3, stream=stream)
+            best_v[kg] = bv
+            tune_ms.update({(kg,) + key: t for key, t in tm.items()})
+        plan = B.BatchGroupPlan(h, mats, kk, best_v)
+        info = {"tiles": None, "warps": None, "groups": plan.info()["batches"]}
+    else:
+        best_v, tune_ms = B.autotune_batch(h, mats, k, xs, ys, repeats=3, stream=stream)
+        plan = B.BatchPlan(h, mats, k, best_v)
+        info = plan.info()
+    plan.set_vectors(xs, ys)
+    plan.exec(1.0, 0.0, B.BATCH_PERSISTENT_GRAPH)
+    stream.synchronize()
+
+    # parity on sampled matrices (all k columns) against the FP64 oracle
+    worst, checked = 0.0, 0
+    for i in np.linspace(0, len(mats) - 1, args.parity_samples).astype(int):
+        A = mats[i]
+        rp = A.d_rowPtr.cpu().numpy()
+        ci = A.d_colIdx[:A.nnz].cpu().numpy()
+        v = A.d_values[:A.nnz].cpu().numpy()
+        ki = kk[i]
+        X = xs[i].cpu().numpy().reshape(A.numCols, ki)
+        Y = ys[i][:A.numRows * ki].cpu().numpy().reshape(A.numRows, ki)
+        for j in range(ki):
+            yr, absum = oracle.spmv_ref(rp, ci, v, np.ascontiguousarray(X[:, j]))
+            worst = max(worst, float(oracle.row_errors(Y[:, j], yr, absum, 1e-5).max()))
+            checked += A.numRows
+    if worst > 1.0:
+        print(f"PARITY FAILURE k={k}: {worst}", file=sys.stderr)
+
+    nbytes = sum(A.nnz * 8 + (A.numRows + 1) * 4 + ki * A.numRows * 4 + ki * d * 4
+                 for A, d, ki in zip(mats, distinct, kk))
+    sumNK = sum(A.nnz * ki for A, ki in zip(mats, kk))
+    times = {}
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    modes = (("persistent_graph", B.BATCH_PERSISTENT_GRAPH, args.steps),
+             ("persistent", B.BATCH_PERSISTENT, args.steps),
+             ("loop", B.BATCH_LOOP, max(3, args.steps // 4)),
+             ("loop_graph", B.BATCH_LOOP_GRAPH, max(3, args.steps // 4)))
+    for name, mode, steps in modes[:1] if compact else modes:
+        for _ in range(args.warmup):
+            plan.exec(1.0, 0.0, mode)
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            plan.exec(1.0, 0.0, mode)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        times[name] = e0.elapsed_time(e1) / steps
+
+    # the plain per-matrix loop a reference user writes: one single-matrix
+    # plan per matrix (default AUTO variant), one SpMV per right-hand side
+    plans = [mx.Plan(h, A) for A in mats]
+    xcols = [xs[i].view(A.numCols, kk[i]).t().contiguous() for i, A in enumerate(mats)]
+    ycols = [torch.empty(kk[i], max(A.numRows, 1), dtype=torch.float32, device=dev) for i, A in enumerate(mats)]
+    plain_steps = max(2, args.steps // 8)
+
+    def plain_once():
+        for p_, xc, yc in zip(plans, xcols, ycols):
+            for j in range(xc.shape[0]):
+                p_.exec(xc[j], yc[j])
+    plain_once()
+    stream.synchronize()
+    for i in np.linspace(0, len(mats) - 1, 4).astype(int):  # same product as the batch
+        A = mats[i]
+        ref = ys[i][:A.numRows * kk[i]].view(A.numRows, kk[i]).t()
+        assert torch.allclose(ycols[i][:, :A.numRows], ref, rtol=1e-4, atol=1e-4), "plain loop mismatch"
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(plain_steps):
+        plain_once()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    times["plain_loop"] = e0.elapsed_time(e1) / plain_steps
+    for p_ in plans:
+        p_.destroy()
+    del plans
+
+    # the same loop through the reference's own entry point: spmv_csr<T>
+    # per matrix and right-hand side (stateless: tiles found every call)
+    opts = mx.spmv_default_opts(stream)
+
+    def stateless_once():
+        for A, xc, yc in zip(mats, xcols, ycols):
+            for j in range(xc.shape[0]):
+                mx.spmv_csr(A, xc[j], yc[j], 1.0, 0.0, opts)
+    stateless_once()
+    stream.synchronize()
+    e0.record(stream)
+    for _ in range(plain_steps):
+        stateless_once()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    times["spmv_csr_loop"] = e0.elapsed_time(e1) / plain_steps
+    del xcols, ycols
+
+    if compact:
+        clocks.stop()
+        ms = max_over_ranks([times["persistent_graph"]], ws, dev)[0]
+        plan.destroy()
+        del Xd, Yd, xs, ys
+        torch.cuda.empty_cache()
+        return {"workload": f"uneven{len(mats)}", "k": k, "matrices": len(mats), "rows": sumR, "nnz": sumN,
+                "algorithmic_bytes": int(nbytes), "variant": best_v, "ms_per_step": round(ms, 5),
+                "value": round(ws * 1e3 / ms, 3), "unit": "batch/s",
+                "kernel_GBps": round(nbytes / (ms * 1e-3) / 1e9, 2),
+                "frac": round(nbytes / (ms * 1e-3) / 1e9 / peak, 4),
+                "ms": {n: round(t, 4) for n, t in times.items()},
+                "speedup_vs_plain_loop": round(times["plain_loop"] / ms, 3),
+                "speedup_vs_spmv_csr_loop": round(times["spmv_csr_loop"] / ms, 3),
+                "note": "persistent launch replayed from a CUDA graph against a loop of single-matrix plans "
+                        "(plain_loop) and a loop of stateless spmv_csr_f32 calls (spmv_csr_loop)",
+                "parity": {"matrices_checked": int(args.parity_samples), "rows_checked": checked,
+                           "max_err_over_bound": worst},
+                "clocks": clocks.summary(), "generate_s": round(gen_s, 2)}
+
+    # end to end: pinned host X in, Y out, persistent graph in between
+    Xh = torch.empty(xn, dtype=torch.float32).pin_memory()
+    Yh = torch.empty(yn, dtype=torch.float32).pin_memory()
+    Xh.copy_(Xd.cpu())
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            Xd.copy_(Xh, non_blocking=True)
+            plan.exec(1.0, 0.0, B.BATCH_PERSISTENT_GRAPH)
+            Yh.copy_(Yd, non_blocking=True)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.steps):
+            Xd.copy_(Xh, non_blocking=True)
+            plan.exec(1.0, 0.0, B.BATCH_PERSISTENT_GRAPH)
+            Yh.copy_(Yd, non_blocking=True)
+        f1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = f0.elapsed_time(f1) / args.steps
+    clocks.stop()
+    times["persistent_graph"], e2e_ms = max_over_ranks([times["persistent_graph"], e2e_ms], ws, dev)
+
+    ms = times["persistent_graph"]
+    achieved = nbytes / (ms * 1e-3) / 1e9
+    line = {"metric": "batched_spmm_batches_per_s", "value": round(ws * 1e3 / ms, 3), "unit": "batch/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 5),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded device generators)",
+            "config": {"workload": f"uneven{args.batch_count}", "k": k,
+                       "k_counts": {str(z): kk.count(z) for z in sorted(set(kk))} if mixed else None,
+                       "matrices": len(mats), "rows": sumR,
+                       "cols": sumC, "nnz": sumN, "algorithmic_bytes": int(nbytes), "tiles": info["tiles"],
+                       "warps": info["warps"], "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": f"replicas{ws}", "generate_s": round(gen_s, 2),
+                       "gflops": round(2 * sumNK / (ms * 1e-3) / 1e9, 2),
+                       "ms": {n: round(t, 4) for n, t in times.items()},
+                       "variant": {str(z): v for z, v in best_v.items()} if mixed else best_v,
+                       "autotune_ms": {",".join(map(str, key)): round(t, 4) for key, t in tune_ms.items()},
+                       "speedup_vs_plain_loop": round(times["plain_loop"] / ms, 3),
+                       "speedup_vs_spmv_csr_loop": round(times["spmv_csr_loop"] / ms, 3),
+                       "spmv_csr_loop": "per matrix and right-hand side: one spmv_csr_f32 call (the reference's "
+                                        "spmv_csr<T>, stateless: CSR5 tiles found per call, 3 launches)",
+                       "plain_loop": "per matrix: one single-matrix plan (default AUTO variant), one "
+                                     "spmv_plan_exec_f32 per right-hand side, 2 launches each",
+                       "speedup_vs_loop": round(times["loop"] / ms, 3),
+                       "speedup_vs_loop_graph": round(times["loop_graph"] / ms, 3)},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                         "kernel": ("batch_tile_kernel<k> + batch_fixup_kernel<k> per k group (one graph)"
+                                    if mixed else f"batch_tile_kernel<{k}> + batch_fixup_kernel<{k}> (graph)"),
+                         "traffic": None},
+            "e2e": {"value": round(ws * 1e3 / e2e_ms, 3), "unit": "batch/s", "h2d_bytes_per_step": int(xn * 4),
+                    "d2h_bytes_per_step": int(yn * 4), "ms_per_step": round(e2e_ms, 5),
+                    "call": ("spmv_batch_group_exec_f32" if mixed else "spmv_batch_exec_f32") +
+                            " (persistent graph) with pinned X/Y copies"},
+            "gpu_launches": 2 * args.steps * (info["groups"] if mixed else 1),
+            "clocks": clocks.summary(),
+            "parity": {"matrices_checked": int(args.parity_samples), "rows_checked": checked,
+                       "max_err_over_bound": worst}}
+    if rank == 0 and not args.no_cpu_baseline:
+        # bounded sample: the reference CPU loop over 64 matrices, k passes each
+        threads = os.cpu_count() or 1
+        idx = np.linspace(0, len(mats) - 1, 64).astype(int)
+        host = []
+        for i in idx:
+            A = mats[i]
+            host.append((A.d_rowPtr.cpu().numpy(), A.d_colIdx[:A.nnz].cpu().numpy(),
+                         A.d_values[:A.nnz].cpu().numpy(), xs[i].cpu().numpy().reshape(A.numCols, kk[i])))
+        nn = sum(int(rp[-1]) * X.shape[1] for rp, _, _, X in host)  # nonzero-columns
+        t = time.perf_counter()
+        for rp, ci, v, X in host:
+            for j in range(X.shape[1]):
+                oracle.cpu_spmv(rp, ci, v, np.ascontiguousarray(X[:, j]), threads=threads)
+        cpu_s = (time.perf_counter() - t) * sumNK / max(nn, 1)
+        line["cpu_baseline"] = {"value": round(1.0 / cpu_s, 4), "unit": "batch/s", "cores": threads,
+                                "kind": "port",
+                                "sample": f"64 of {len(mats)} matrices ({nn} nonzero-columns), reference CPU "
+                                          f"loop per column, scaled to the batch's {sumNK} nonzero-columns"}
+    plan.destroy()
+    del Xd, Yd, xs, ys, Xh, Yh
+    torch.cuda.empty_cache()
+    return line
 
 
 def batched_arm(args):
@@ -655,222 +938,13 @@ def batched_arm(args):
     sumR = sum(A.numRows for A in mats)
     sumC = sum(A.numCols for A in mats)
     peak, peak_kind = peaks()
-    L = mx.lib()
-
-    def aligned_slices(sizes):
-        offs, o = [], 0
-        for n in sizes:
-            offs.append(o)
-            o += (n + 3) // 4 * 4
-        return offs, max(o, 4)
-
+    ctx = dict(mx=mx, B=B, oracle=oracle, h=h, stream=stream, dev=dev, mats=mats, distinct=distinct,
+               rank=rank, ws=ws, local=local, peak=peak, peak_kind=peak_kind, gen_s=gen_s, sumR=sumR, sumC=sumC,
+               sumN=sumN)
     for kspec in args.k.split(","):
-        # "mixed": each matrix draws its own k from {1, 2, 4, 8, 16} (seeded);
-        # the batch runs as a group of single-k batches in one graph
-        mixed = kspec == "mixed"
-        if mixed:
-            kk = [int(z) for z in np.random.default_rng(4242 + rank).choice([1, 2, 4, 8, 16], len(mats))]
-            k = "mixed"
-        else:
-            k = int(kspec)
-            kk = [k] * len(mats)
-        xo, xn = aligned_slices([A.numCols * ki for A, ki in zip(mats, kk)])
-        yo, yn = aligned_slices([A.numRows * ki for A, ki in zip(mats, kk)])
-        Xd = torch.empty(xn, dtype=torch.float32, device=dev)
-        Yd = torch.empty(yn, dtype=torch.float32, device=dev)
-        mx.check(L.spmv_gen_device_vector_f32(xn, 1000 + (0 if mixed else k), -1.0, 1.0, Xd.data_ptr(), None),
-                 "gen x")
-        xs = [Xd[o:o + A.numCols * ki] for o, A, ki in zip(xo, mats, kk)]
-        ys = [Yd[o:o + max(A.numRows * ki, 1)] for o, A, ki in zip(yo, mats, kk)]
-        # launch shape picked by the batch autotuner on this batch (per k group)
-        if mixed:
-            best_v, tune_ms = {}, {}
-            for kg in sorted(set(kk)):
-                sel_ = [i for i, ki in enumerate(kk) if ki == kg]
-                bv, tm = B.autotune_batch(h, [mats[i] for i in sel_], kg, [xs[i] for i in sel_],
-                                          [ys[i] for i in sel_], repeats=3, stream=stream)
-                best_v[kg] = bv
-                tune_ms.update({(kg,) + key: t for key, t in tm.items()})
-            plan = B.BatchGroupPlan(h, mats, kk, best_v)
-            info = {"tiles": None, "warps": None, "groups": plan.info()["batches"]}
-        else:
-            best_v, tune_ms = B.autotune_batch(h, mats, k, xs, ys, repeats=3, stream=stream)
-            plan = B.BatchPlan(h, mats, k, best_v)
-            info = plan.info()
-        plan.set_vectors(xs, ys)
-        plan.exec(1.0, 0.0, B.BATCH_PERSISTENT_GRAPH)
-        stream.synchronize()
-
-        # parity on sampled matrices (all k columns) against the FP64 oracle
-        worst, checked = 0.0, 0
-        for i in np.linspace(0, len(mats) - 1, args.parity_samples).astype(int):
-            A = mats[i]
-            rp = A.d_rowPtr.cpu().numpy()
-            ci = A.d_colIdx[:A.nnz].cpu().numpy()
-            v = A.d_values[:A.nnz].cpu().numpy()
-            ki = kk[i]
-            X = xs[i].cpu().numpy().reshape(A.numCols, ki)
-            Y = ys[i][:A.numRows * ki].cpu().numpy().reshape(A.numRows, ki)
-            for j in range(ki):
-                yr, absum = oracle.spmv_ref(rp, ci, v, np.ascontiguousarray(X[:, j]))
-                worst = max(worst, float(oracle.row_errors(Y[:, j], yr, absum, 1e-5).max()))
-                checked += A.numRows
-        if worst > 1.0:
-            print(f"PARITY FAILURE k={k}: {worst}", file=sys.stderr)
-
-        nbytes = sum(A.nnz * 8 + (A.numRows + 1) * 4 + ki * A.numRows * 4 + ki * d * 4
-                     for A, d, ki in zip(mats, distinct, kk))
-        sumNK = sum(A.nnz * ki for A, ki in zip(mats, kk))
-        times = {}
-        clocks = ClockSampler(local)
-        clocks.start()
-        time.sleep(0.3)
-        for name, mode, steps in (("persistent_graph", B.BATCH_PERSISTENT_GRAPH, args.steps),
-                                  ("persistent", B.BATCH_PERSISTENT, args.steps),
-                                  ("loop", B.BATCH_LOOP, max(3, args.steps // 4)),
-                                  ("loop_graph", B.BATCH_LOOP_GRAPH, max(3, args.steps // 4))):
-            for _ in range(args.warmup):
-                plan.exec(1.0, 0.0, mode)
-            stream.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(steps):
-                plan.exec(1.0, 0.0, mode)
-            e1.record(stream)
-            torch.cuda.synchronize(dev)
-            times[name] = e0.elapsed_time(e1) / steps
-
-        # the plain per-matrix loop a reference user writes: one single-matrix
-        # plan per matrix (default AUTO variant), one SpMV per right-hand side
-        plans = [mx.Plan(h, A) for A in mats]
-        xcols = [xs[i].view(A.numCols, kk[i]).t().contiguous() for i, A in enumerate(mats)]
-        ycols = [torch.empty(kk[i], max(A.numRows, 1), dtype=torch.float32, device=dev) for i, A in enumerate(mats)]
-        plain_steps = max(2, args.steps // 8)
-
-        def plain_once():
-            for p_, xc, yc in zip(plans, xcols, ycols):
-                for j in range(xc.shape[0]):
-                    p_.exec(xc[j], yc[j])
-        plain_once()
-        stream.synchronize()
-        for i in np.linspace(0, len(mats) - 1, 4).astype(int):  # same product as the batch
-            A = mats[i]
-            ref = ys[i][:A.numRows * kk[i]].view(A.numRows, kk[i]).t()
-            assert torch.allclose(ycols[i][:, :A.numRows], ref, rtol=1e-4, atol=1e-4), "plain loop mismatch"
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(plain_steps):
-            plain_once()
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        times["plain_loop"] = e0.elapsed_time(e1) / plain_steps
-        for p_ in plans:
-            p_.destroy()
-        del plans
-
-        # the same loop through the reference's own entry point: spmv_csr<T>
-        # per matrix and right-hand side (stateless: tiles found every call)
-        opts = mx.spmv_default_opts(stream)
-
-        def stateless_once():
-            for A, xc, yc in zip(mats, xcols, ycols):
-                for j in range(xc.shape[0]):
-                    mx.spmv_csr(A, xc[j], yc[j], 1.0, 0.0, opts)
-        stateless_once()
-        stream.synchronize()
-        e0.record(stream)
-        for _ in range(plain_steps):
-            stateless_once()
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        times["spmv_csr_loop"] = e0.elapsed_time(e1) / plain_steps
-        del xcols, ycols
-
-        # end to end: pinned host X in, Y out, persistent graph in between
-        Xh = torch.empty(xn, dtype=torch.float32).pin_memory()
-        Yh = torch.empty(yn, dtype=torch.float32).pin_memory()
-        Xh.copy_(Xd.cpu())
-        with torch.cuda.stream(stream):
-            for _ in range(args.warmup):
-                Xd.copy_(Xh, non_blocking=True)
-                plan.exec(1.0, 0.0, B.BATCH_PERSISTENT_GRAPH)
-                Yh.copy_(Yd, non_blocking=True)
-            f0 = torch.cuda.Event(enable_timing=True)
-            f1 = torch.cuda.Event(enable_timing=True)
-            f0.record(stream)
-            for _ in range(args.steps):
-                Xd.copy_(Xh, non_blocking=True)
-                plan.exec(1.0, 0.0, B.BATCH_PERSISTENT_GRAPH)
-                Yh.copy_(Yd, non_blocking=True)
-            f1.record(stream)
-        torch.cuda.synchronize(dev)
-        e2e_ms = f0.elapsed_time(f1) / args.steps
-        clocks.stop()
-        times["persistent_graph"], e2e_ms = max_over_ranks([times["persistent_graph"], e2e_ms], ws, dev)
-
-        ms = times["persistent_graph"]
-        achieved = nbytes / (ms * 1e-3) / 1e9
-        line = {"metric": "batched_spmm_batches_per_s", "value": round(ws * 1e3 / ms, 3), "unit": "batch/s",
-                "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 5),
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded device generators)",
-                "config": {"workload": f"uneven{args.batch_count}", "k": k,
-                           "k_counts": {str(z): kk.count(z) for z in sorted(set(kk))} if mixed else None,
-                           "matrices": len(mats), "rows": sumR,
-                           "cols": sumC, "nnz": sumN, "algorithmic_bytes": int(nbytes), "tiles": info["tiles"],
-                           "warps": info["warps"], "l2": "inputs larger than L2 (no flush)",
-                           "parallelism": f"replicas{ws}", "generate_s": round(gen_s, 2),
-                           "gflops": round(2 * sumNK / (ms * 1e-3) / 1e9, 2),
-                           "ms": {n: round(t, 4) for n, t in times.items()},
-                           "variant": {str(z): v for z, v in best_v.items()} if mixed else best_v,
-                           "autotune_ms": {",".join(map(str, key)): round(t, 4) for key, t in tune_ms.items()},
-                           "speedup_vs_plain_loop": round(times["plain_loop"] / ms, 3),
-                           "speedup_vs_spmv_csr_loop": round(times["spmv_csr_loop"] / ms, 3),
-                           "spmv_csr_loop": "per matrix and right-hand side: one spmv_csr_f32 call (the reference's "
-                                            "spmv_csr<T>, stateless: CSR5 tiles found per call, 3 launches)",
-                           "plain_loop": "per matrix: one single-matrix plan (default AUTO variant), one "
-                                         "spmv_plan_exec_f32 per right-hand side, 2 launches each",
-                           "speedup_vs_loop": round(times["loop"] / ms, 3),
-                           "speedup_vs_loop_graph": round(times["loop_graph"] / ms, 3)},
-                "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                             "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                             "kernel": ("batch_tile_kernel<k> + batch_fixup_kernel<k> per k group (one graph)"
-                                        if mixed else f"batch_tile_kernel<{k}> + batch_fixup_kernel<{k}> (graph)"),
-                             "traffic": None},
-                "e2e": {"value": round(ws * 1e3 / e2e_ms, 3), "unit": "batch/s", "h2d_bytes_per_step": int(xn * 4),
-                        "d2h_bytes_per_step": int(yn * 4), "ms_per_step": round(e2e_ms, 5),
-                        "call": ("spmv_batch_group_exec_f32" if mixed else "spmv_batch_exec_f32") +
-                                " (persistent graph) with pinned X/Y copies"},
-                "gpu_launches": 2 * args.steps * (info["groups"] if mixed else 1),
-                "clocks": clocks.summary(),
-                "parity": {"matrices_checked": int(args.parity_samples), "rows_checked": checked,
-                           "max_err_over_bound": worst}}
-        if rank == 0 and not args.no_cpu_baseline:
-            # bounded sample: the reference CPU loop over 64 matrices, k passes each
-            threads = os.cpu_count() or 1
-            idx = np.linspace(0, len(mats) - 1, 64).astype(int)
-            host = []
-            for i in idx:
-                A = mats[i]
-                host.append((A.d_rowPtr.cpu().numpy(), A.d_colIdx[:A.nnz].cpu().numpy(),
-                             A.d_values[:A.nnz].cpu().numpy(), xs[i].cpu().numpy().reshape(A.numCols, kk[i])))
-            nn = sum(int(rp[-1]) * X.shape[1] for rp, _, _, X in host)  # nonzero-columns
-            t = time.perf_counter()
-            for rp, ci, v, X in host:
-                for j in range(X.shape[1]):
-                    oracle.cpu_spmv(rp, ci, v, np.ascontiguousarray(X[:, j]), threads=threads)
-            cpu_s = (time.perf_counter() - t) * sumNK / max(nn, 1)
-            line["cpu_baseline"] = {"value": round(1.0 / cpu_s, 4), "unit": "batch/s", "cores": threads,
-                                    "kind": "port",
-                                    "sample": f"64 of {len(mats)} matrices ({nn} nonzero-columns), reference CPU "
-                                              f"loop per column, scaled to the batch's {sumNK} nonzero-columns"}
+        line = batch_k_line(args, ctx, kspec)
         if rank == 0:
             print(json.dumps(line), flush=True)
-        plan.destroy()
-        del Xd, Yd, xs, ys, Xh, Yh
-        torch.cuda.empty_cache()
     h.destroy()
     if ws > 1:
         dist.destroy_process_group()

@@ -550,7 +550,7 @@ SPMV_API spmv_status_t spmv_plan_inject_wait_timeout(spmv_plan_t plan, int enabl
  * batches, selector models, stateless scratch -- is counted while live:
  * spmv_debug_device_memory reports the live bytes and allocations.
  * spmv_debug_fail_allocation(n), n >= 1: the n-th device allocation from now
- * fails as if the device were out of memory (the driver is not asked); the
+ * fails as if the device were out of memory (the CUDA driver is not asked); the
  * call that made it returns SPMV_ERROR_MEMORY_ALLOC after releasing what it
  * had taken.  n = 0 turns injection off.  Process-wide, not thread-local. */
 SPMV_API spmv_status_t spmv_debug_fail_allocation(long long n);

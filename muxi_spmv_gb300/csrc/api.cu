@@ -69,7 +69,7 @@ int current_sm_count() {
 // ---------------------------------------------------------------------------
 // Stream-ordered scratch: one memory pool per device that keeps its memory
 // between calls (release threshold = unlimited), so repeated stateless calls
-// do not return memory to the driver and re-map it.
+// do not return memory to the CUDA driver and re-map it.
 // ---------------------------------------------------------------------------
 static std::mutex g_pool_mu;
 static std::vector<cudaMemPool_t> g_pools;

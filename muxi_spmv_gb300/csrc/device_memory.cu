@@ -2,7 +2,7 @@
 // (a) count the live allocations and bytes, so a test can show that a call
 // that failed half-way released everything it had taken, and (b) can be told
 // to fail the n-th allocation from now with cudaErrorMemoryAllocation,
-// without asking the driver, so the library's out-of-memory paths run on any
+// without asking the CUDA driver, so the library's out-of-memory paths run on any
 // machine.  Neither changes what a successful call does.
 #include <atomic>
 #include <mutex>

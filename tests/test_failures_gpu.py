@@ -6,7 +6,7 @@ allocation is made to fail for n = 1, 2, ... until the call succeeds.  Every
 failing attempt must return SPMV_ERROR_MEMORY_ALLOC (the reference's status
 value, src/utils/common.h:31-43) and leave the library's live device memory
 exactly where it was; the attempt that succeeds must give the oracle's
-result.  No GPU fault is involved: the driver is never asked for the failing
+result.  No GPU fault is involved: the CUDA driver is never asked for the failing
 allocation."""
 from __future__ import annotations
 
