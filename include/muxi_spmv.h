@@ -238,8 +238,8 @@ SPMV_API spmv_status_t spmv_bsr_f64(int numRows, int numCols, int B, int numBloc
  * SPMV_ERROR_MEMORY_ALLOC and a message that states the limit.  Every GPU
  * that loads the library keeps that array until the process exits.  The
  * first call on a device looks up the array's address (cudaGetSymbolAddress)
- * and keeps it; make that call before any stream capture, and do not use the
- * entry point on a device after cudaDeviceReset.  All calls share the one
+ * and keeps it; do not use the entry point on a device after
+ * cudaDeviceReset.  All calls share the one
  * array, which keeps the last call's contents (nothing in it needs to start
  * at zero): calls that can overlap on the GPU (different streams without
  * ordering) race and must be serialised by the caller. */

@@ -10,8 +10,7 @@
 // kNoAllocScratchBytes.  Every GPU that loads this library reserves that
 // array for the life of the process.  Its device address is looked up with
 // cudaGetSymbolAddress once per device, on the first call made with that
-// device current; make that first call before any stream capture.  The
-// address stays cached for the process: after a cudaDeviceReset the module is
+// device current.  The address stays cached for the process: after a cudaDeviceReset the module is
 // reloaded and the array may move, so do not call this entry point on a
 // device that has been reset.
 #include <mutex>
