@@ -255,7 +255,7 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
         T sum = T(0);
 #pragma unroll
         for (int e = 0; e < E; ++e) sum += L.v[e] * g[e];
-        sum = group_sum<32>(sum);
+        sum = warp_sum_exact(sum);  // FP32: the shuffle butterfly
         if (lane == 0) {
             carryRow[t] = rFirst;
             carryVal[t] = sum;

@@ -154,6 +154,51 @@ __device__ __forceinline__ T group_sum(T v) {
     return v;
 }
 
+// Full-warp sum of one double per lane, returned to every lane, computed with
+// integer reductions instead of FP64 adds (GB300 runs FP64 arithmetic at
+// about two lanes per clock per SM, so five FP64 adds per warp sum cost as
+// much as five of a tile's eight FMAs).  Every lane's value is truncated to
+// a multiple of 2^(emax - 1079), emax the largest biased exponent in the
+// warp, so |V| < 2^57 and the 32-lane sum fits an int64; V is split into
+// three fields of 21 unsigned, 21 unsigned and 15 signed bits, each summed
+// exactly by redux.sync.  The result is that fixed-point sum rounded once to
+// the nearest double (ties to even).  Error: under 32 units of 2^(emax -
+// 1079), i.e. below 2^-51 of the largest lane's magnitude, which is no more
+// than the sum of the lanes' magnitudes.  Infinities, NaNs and exponents
+// near the ends of the range (emax < 64 or > 2040) take the FP64 butterfly.
+__device__ __forceinline__ double fixed_to_double(long long t, unsigned emax) {
+    if (t == 0) return 0.0;
+    const unsigned long long sign = t < 0 ? (1ull << 63) : 0ull;
+    unsigned long long m = t < 0 ? 0ull - (unsigned long long)t : (unsigned long long)t;
+    const int lz = __clzll((long long)m);  // m < 2^62: lz >= 2
+    m <<= lz;                              // leading one at bit 63
+    unsigned long long mant = m >> 11;     // 53 bits, leading one at bit 52
+    const unsigned long long rest = m & 0x7ffull;
+    if (rest > 0x400ull || (rest == 0x400ull && (mant & 1ull))) ++mant;
+    long long be = (long long)emax + 7 - lz;  // value = (m / 2^63) * 2^(63 - lz) * 2^(emax - 1079)
+    if (mant >> 53) {
+        mant >>= 1;
+        ++be;
+    }
+    return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | (mant & 0xfffffffffffffull)));
+}
+
+__device__ __forceinline__ double warp_sum_exact(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    const unsigned emax = __reduce_max_sync(kFull, e);
+    if (emax == 0x7ffu || emax < 64u || emax > 2040u) return group_sum<32>(v);  // warp-uniform
+    const unsigned long long m = (b & 0xfffffffffffffull) | (e ? (1ull << 52) : 0ull);
+    const unsigned d = emax - (e ? e : 1u);
+    long long V = d >= 57u ? 0ll : (long long)((m << 4) >> d);
+    if (b >> 63) V = -V;
+    const unsigned lo = __reduce_add_sync(kFull, (unsigned)V & 0x1fffffu);
+    const unsigned mid = __reduce_add_sync(kFull, (unsigned)(V >> 21) & 0x1fffffu);
+    const int hi = (int)__reduce_add_sync(kFull, (unsigned)(int)(V >> 42));
+    return fixed_to_double(((long long)hi << 42) + ((long long)mid << 21) + (long long)lo, emax);
+}
+__device__ __forceinline__ float warp_sum_exact(float v) { return group_sum<32>(v); }
+
 // ---------------------------------------------------------------------------
 // mbarrier and bulk-copy (TMA) helpers, CTA scope.
 // ---------------------------------------------------------------------------

@@ -305,6 +305,42 @@ def test_plans(mx, cuda, handle, cases):
     p.destroy()
 
 
+def test_f64_interior_tiles_over_wide_exponent_ranges(mx, cuda, handle):
+    """FP64 tiles inside one row sum their lanes in 64-bit fixed point below
+    the largest lane's exponent: long rows whose products span 1e-300 to
+    1e300, cancel to a small remainder, sit near the top of the range, or are
+    tiny enough to take the FP64 fallback, each within the FP64 bound; a row
+    of integer products comes out exact."""
+    torch = cuda
+    rng = np.random.default_rng(57)
+    cols = 60_000
+    lens = [40_000, 20_000, 12_000, 12_000, 9_000] + [int(z) for z in rng.integers(1, 40, 500)]
+    rp = np.r_[0, np.cumsum(lens)].astype(np.int32)
+    ci = np.concatenate([np.sort(rng.choice(cols, l, replace=False)) for l in lens]).astype(np.int32)
+    v = rng.standard_normal(rp[-1])
+    s0, s1, s2, s3, s4 = (slice(rp[i], rp[i + 1]) for i in range(5))
+    v[s0] *= 10.0 ** rng.uniform(-300, 300, lens[0])  # products over 600 decades
+    v[s1] = np.where(np.arange(lens[1]) % 2 == 0, 1e16, -1e16) * (1 + 1e-12 * rng.standard_normal(lens[1]))
+    v[s2] *= 1e-305                                   # tiny: largest exponent below the fixed-point range
+    v[s3] *= 1e300                                    # near the top of the range
+    v[s4] = rng.integers(-1000, 1001, lens[4]).astype(np.float64)
+    xh = rng.uniform(-1, 1, cols)
+    xh[ci[s4]] = rng.integers(-3, 4, lens[4]).astype(np.float64)  # row 4: integer products
+    A = device_csr(mx, rp, ci, v, cols)
+    x = torch.from_numpy(xh).cuda()
+    exact4 = int(np.sum(v[s4].astype(np.int64) * xh[ci[s4]].astype(np.int64)))
+    R = mx.RANGE_PER_RESIDENT_BLOCK
+    for var in (None, mx.make_variant(mx.KERNEL_CSR5, 128, 0, 16, 32), mx.make_variant(mx.KERNEL_CSR5, 128, 0, 8, 32),
+                mx.make_variant(mx.KERNEL_CSR5, 1024, R, 8, mx.CSR5_ORDERED_PREFETCH)):
+        p = mx.Plan(handle, A, var)
+        y = torch.zeros(A.numRows, dtype=torch.float64, device="cuda")
+        p.exec(x, y)
+        torch.cuda.synchronize()
+        check(y, np.zeros(A.numRows), A, xh, 1.0, 0.0)
+        assert y[4].item() == float(exact4)
+        p.destroy()
+
+
 def test_unused_nonfinite_x_does_not_leak(mx, cuda, handle):
     """Padding slots and masked lanes read x[0] or other columns without using
     them: an Inf / NaN in columns no nonzero references must not reach y."""
