@@ -350,7 +350,7 @@ def selector_record(args, mx, h, A, x, y, stream, dev):
             "cost_ratio": round(autotune_s / max(learned_s, 1e-9), 1),
             "fallback_cost_ratio": round(autotune_s / max(fallback_s, 1e-9), 1),
             "note": "selection = spmv_select (features + MLP forward + rank), the same with the variants "
-                    "predicted within 5% timed (the mode of the benchmark's AUTO plans), and "
+                    "predicted within 12% timed, at most four (the mode of the benchmark's AUTO plans), and "
                     "spmv_select(AUTOTUNE) (every applicable variant timed as a plan); regrets from the picks' "
                     "plans timed back to back with CUDA events"}
 
@@ -386,7 +386,7 @@ def gpu_arm(args):
         from muxi_spmv_gb300 import selector as S
         model = S.MLP.load(S.DEFAULT_MODEL)
         # AUTO plans take the learned pick; with the fallback, the variants
-        # predicted within 5% of it are timed at plan creation and the fastest kept
+        # predicted within 12% of it (at most four) are timed at plan creation and the fastest kept
         S.set_selector(h, model, S.SELECT_LEARNED_FALLBACK if args.select == "learned_fallback" else S.SELECT_LEARNED)
     perm = None
     if args.colperm != "none":
@@ -966,7 +966,7 @@ def main():
                     help="skip the other configurations and the selector record (profiling runs)")
     ap.add_argument("--select", default="learned_fallback", choices=["default", "learned", "learned_fallback"],
                     help="AUTO plan: the fixed default variant, the learned selector's pick, or that pick with the "
-                         "variants predicted within 5%% of it timed at plan creation")
+                         "variants predicted within 12%% of it (at most four) timed at plan creation")
     ap.add_argument("--slices", type=int, default=1, help="host pipeline row slices")
     ap.add_argument("--depth", type=int, default=2, help="host pipeline requests in flight")
     ap.add_argument("--scale-rows", type=int, default=0, help="same law on this many rows (profiling cases)")

@@ -263,7 +263,9 @@ typedef enum {
     SPMV_KERNEL_BAND = 7,      /* ordered CSR5 tiles of 32*itemsPerThread nonzeros; each
                                   CTA owns a range of consecutive tiles and serves the
                                   gathers that fall in a bulk-copied shared-memory
-                                  window of x around its rows from there            */
+                                  window of x around its rows from there (FP32 at
+                                  1024 threads and 8 per lane: one CTA per SM, the
+                                  next tile's loads in flight)                      */
     SPMV_KERNEL_STREAM = 8     /* ordered CSR5 tiles of 32*itemsPerThread nonzeros, one
                                   CTA per SM over a contiguous tile range; each warp's
                                   next tiles are bulk-copied (TMA) into a ring of
@@ -310,7 +312,8 @@ typedef struct {
                             before the current tile's compute (block ranges
                             of 512, 768 or 1024 threads);
                             BAND: x window in units of 1,024 elements
-                            (0: the largest the CTA shape fits)           */
+                            (0: 16, or the largest the CTA shape fits if
+                            smaller)                                      */
 } spmv_variant_t;
 
 /* Run one explicit variant (no plan, no selector).  MERGE variants take
@@ -749,9 +752,10 @@ typedef enum {
     SPMV_SELECT_AUTOTUNE = 2,      /* time the whole space                      */
     SPMV_SELECT_LEARNED_TOPK = 3,  /* time only the model's topK best guesses   */
     SPMV_SELECT_LEARNED_FALLBACK = 4 /* learned pick; when other variants are
-                                        predicted within 5% of it (low
+                                        predicted within 12% of it (low
                                         confidence), time those too (at most
-                                        topK, default 3) and take the fastest */
+                                        topK candidates, default 4) and take
+                                        the fastest */
 } spmv_select_mode_t;
 
 /* Picks a variant for a device CSR matrix.  `model` is needed by the
@@ -770,7 +774,7 @@ SPMV_API spmv_status_t spmv_set_selector(spmv_handle_t* handle, spmv_mlp_t model
 /* How AUTO plans on this handle use the registered model:
  * SPMV_SELECT_LEARNED (default: the model's pick, about 0.15 ms) or
  * SPMV_SELECT_LEARNED_FALLBACK (plan creation also times the variants
- * predicted within 5% of the pick). */
+ * predicted within 12% of the pick, at most four candidates). */
 SPMV_API spmv_status_t spmv_set_selector_mode(spmv_handle_t* handle, spmv_select_mode_t mode);
 
 /* ------------------------------------------------------------------ */

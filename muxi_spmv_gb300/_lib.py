@@ -229,7 +229,8 @@ BATCH_PERSISTENT, BATCH_PERSISTENT_GRAPH, BATCH_LOOP, BATCH_LOOP_GRAPH = range(4
 
 NUM_FEATURES = 32
 SELECT_HEURISTIC, SELECT_LEARNED, SELECT_AUTOTUNE, SELECT_LEARNED_TOPK, SELECT_LEARNED_FALLBACK = range(5)
-FALLBACK_MARGIN = 0.05  # predicted log-time gap of SELECT_LEARNED_FALLBACK (select.cu)
+FALLBACK_MARGIN = 0.12  # predicted log-time gap of SELECT_LEARNED_FALLBACK (select.cu)
+FALLBACK_MAX = 4  # candidates it times at most, the pick included (select.cu)
 
 _lib = None
 

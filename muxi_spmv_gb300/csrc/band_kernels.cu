@@ -11,14 +11,19 @@
 // the window reads shared memory; every other gather reads x from global
 // memory, so the window changes only speed, never results.
 //
-// Why: on matrices whose columns cluster near the diagonal (the 70% near
-// share of the power-law workload, stencils, banded matrices), the gathers of
-// one tile touch a few hundred distinct x sectors that neighbouring tiles on
-// other SMs touch again.  Each such gather is an L1 miss request to L2, and
-// that request path is the busiest unit of the one-tile-per-warp kernel.  The
-// window turns those gathers into shared-memory reads: the x slice crosses
-// from L2 once per CTA (one bulk copy of W elements for perBlock * sigma
-// nonzeros), and only the far gathers still go to L2.
+// Why: random gathers of 32 lanes ran at about 330 G/s from L2-resident x,
+// 880 G/s from L1-resident x and 2,130 G/s from shared memory on GB300 (one
+// CTA of 1,024 threads per SM, 8 independent gathers per thread): a global
+// gather costs the L1 about one tag lookup per lane, a shared one a few bank
+// wavefronts per instruction.  On matrices whose columns cluster near the
+// diagonal (the 70% near share of the power-law workload, stencils, banded
+// matrices) the window turns most gathers into shared-memory reads; the x
+// slice crosses from L2 once per CTA (one bulk copy of W elements for
+// perBlock * sigma nonzeros), and only the far gathers still go to the L1.
+// The window and the hand-off regions come out of the same on-chip memory as
+// the L1, where the far gathers and the matrix stream's loads in flight
+// land, so the launch asks for no more shared memory than it uses (the
+// carve-out below) and windows of 14-20K elements beat larger ones.
 //
 // Window placement: the CTA's rows [R0, R1] map to columns by the aspect
 // ratio C/R; the window of `winCap` elements is centred there and clamped to
@@ -43,20 +48,37 @@
 namespace mxs {
 
 // Gather through the CTA's window: columns in [lo, lo + span) from shared
-// memory, all others from global memory.  One generic load per gather: the
-// lane picks the address (window slot or x + c) and the load unit routes
-// shared-window addresses to shared memory and the rest to global memory, so
-// a lane's E gathers stay independent loads in flight together, each with
-// one destination register.
+// memory, all others from global memory.  With a window each lane executes
+// exactly one of two complementary predicated loads (ld.shared for window
+// columns, ld.global.nc for the rest): a shared-memory gather of 32 lanes
+// costs a few bank wavefronts where a global one costs about one L1 tag
+// lookup per lane, and only the lanes outside the window reach the L1.
+// Without one (span = 0: x not 16-byte aligned) it is the plain read-only
+// load.  The test on span is also measured to matter for speed: with it the
+// compiler keeps each gather apart from the surrounding work (4,550 against
+// 4,450 GB/s on the 8M-row power law without it).  What keeps the shared
+// loads after the wait for the window's bulk copy is their input `span`,
+// which passes through a volatile move placed after that wait.
 template <typename T>
 struct WindowGather {
     const T* __restrict__ x;
-    const T* win;  // generic address of the window
+    unsigned win;  // shared-window address of the window
     int lo, span;
     __device__ __forceinline__ T operator()(int c) const {
+        if (span == 0) return ld_x(x + c);
         const unsigned o = (unsigned)(c - lo);
-        const T* p = o < (unsigned)span ? win + o : x + c;
-        return *p;
+        T r;
+        if constexpr (sizeof(T) == 4)
+            asm("{\n\t.reg .pred p;\n\tsetp.lt.u32 p, %1, %2;\n\t@p ld.shared.f32 %0, [%3];\n\t"
+                "@!p ld.global.nc.f32 %0, [%4];\n\t}"
+                : "=f"(r)
+                : "r"(o), "r"((unsigned)span), "r"(win + 4u * o), "l"(x + c));
+        else
+            asm("{\n\t.reg .pred p;\n\tsetp.lt.u32 p, %1, %2;\n\t@p ld.shared.f64 %0, [%3];\n\t"
+                "@!p ld.global.nc.f64 %0, [%4];\n\t}"
+                : "=d"(r)
+                : "r"(o), "r"((unsigned)span), "r"(win + 8u * o), "l"(x + c));
+        return r;
     }
 };
 
@@ -96,7 +118,7 @@ __device__ __forceinline__ bool window_wait(unsigned long long* bar, long long l
 // tiles one at a time from a shared counter (neighbouring rows in flight
 // together, no block waits on one long tile).  Dynamic shared memory: the
 // window, winCap elements.
-template <typename T, int E, int BLOCK, int MINB>
+template <typename T, int E, int BLOCK, int MINB, bool PF = false>
 __global__ void __launch_bounds__(BLOCK, MINB)
 csr5_window_kernel(int numRows, int numCols, int nnz, const int* __restrict__ rowPtr,
                    const int* __restrict__ colIdx, const T* __restrict__ values, const T* __restrict__ x,
@@ -131,7 +153,7 @@ csr5_window_kernel(int numRows, int numCols, int nnz, const int* __restrict__ ro
         mbar_arrive_expect_tx(&bar, (unsigned)(span * sizeof(T)));
         bulk_g2s(win, x + lo, (unsigned)(span * sizeof(T)), &bar);
     }
-    const WindowGather<T> gather{x, win, lo, span};
+
     const bool bz = betaZero != 0, plain = betaZero == kPlainAxpby;
     const bool useBits = tileBits != nullptr, noEmpty = noEmptyRows != 0;
 
@@ -140,6 +162,24 @@ csr5_window_kernel(int numRows, int numCols, int nnz, const int* __restrict__ ro
     if (t < te) csr5_ordered_load<T, E>(L, t, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
     // every thread waits (also warps without a tile: the CTA stays until the copy has landed)
     if (span > 0 && !window_wait(&bar, waitLimit, inject, errFlag)) return;
+    int spanAfterWait = span;
+    asm volatile("mov.b32 %0, %0;" : "+r"(spanAfterWait));  // orders every window read after the wait
+    const WindowGather<T> gather{x, smem_u32(win), lo, spanAfterWait};
+    if constexpr (PF) {  // the next tile's loads in flight during this tile's gathers and row logic
+        OrderedLoad<T, E> nxt;
+        while (t < te) {
+            int next = 0;
+            if (lane == 0) next = atomicAdd(&sNext, 1);
+            next = __shfl_sync(kFull, next, 0);
+            if (next < te)
+                csr5_ordered_load<T, E>(nxt, next, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
+            csr5_ordered_compute<T, E, true>(L, t, lane, nnz, rowPtr, gather, y, alpha, beta, bz, tiles, carryRow,
+                                             carryVal, noEmpty, sRpAll[w], sPAll[w], useBits, plain);
+            L = nxt;
+            t = next;
+        }
+        return;
+    }
     while (t < te) {
         int next = 0;  // drawn before the compute so its latency hides under the gathers
         if (lane == 0) next = atomicAdd(&sNext, 1);
@@ -156,7 +196,7 @@ bool band_shape_supported(int block, int E) {
 
 // Default window capacity (elements) of a shape: the largest multiple of
 // 1,024 elements that keeps MINB CTAs per SM within the SM's shared memory
-// (228 KB, 1 KB of it reserved per CTA), capped at 32,768.
+// (228 KB, 1 KB of it reserved per CTA), capped at 40,960.
 template <typename T, int E, int BLOCK, int MINB>
 static int default_window(const DeviceProps& dp) {
     constexpr size_t staticBytes = (BLOCK / 32) * (kOrderedRpCap * sizeof(int) + ordered_slots<T, E>() * sizeof(T)) + 64;
@@ -165,32 +205,46 @@ static int default_window(const DeviceProps& dp) {
     size_t room = perCta > staticBytes ? perCta - staticBytes : 0;
     if (dp.smem_optin && room + staticBytes > dp.smem_optin) room = dp.smem_optin - staticBytes;
     long long elems = (long long)(room / sizeof(T)) / 1024 * 1024;
-    if (elems > 32768) elems = 32768;
+    if (elems > 40960) elems = 40960;
     return (int)(elems < 0 ? 0 : elems);
 }
 
-template <typename T, int E, int BLOCK, int MINB>
+template <typename T, int E, int BLOCK, int MINB, bool PF = false>
 static spmv_status_t launch_window(const int* tileRow, long long tiles, int* carryRow, T* carryVal, int* errFlag,
                                    const RowsArgs<T>& a, int numCols, int tilesPerWarp, int winK,
                                    const unsigned* bits, const BandTest& test, cudaStream_t s) {
-    auto kern = csr5_window_kernel<T, E, BLOCK, MINB>;
+    auto kern = csr5_window_kernel<T, E, BLOCK, MINB, PF>;
     int dev = 0;
     MXS_CUDA(cudaGetDevice(&dev));
     const DeviceProps& dp = device_props(dev);
     const int maxWin = default_window<T, E, BLOCK, MINB>(dp);
-    int cap = winK > 0 ? winK * 1024 : maxWin;
+    int cap = winK > 0 ? winK * 1024 : 16384;
     if (cap > maxWin) cap = maxWin;
     const bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0;
     if (!aligned) cap = 0;
     static bool attrSet[64] = {false};
+    static size_t staticSmem = 0;
     if (dev >= 64 || !attrSet[dev]) {
         MXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)(sizeof(T) * (size_t)maxWin > 16 ? sizeof(T) * (size_t)maxWin : 16)));
-        MXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        cudaFuncAttributes fa{};
+        MXS_CUDA(cudaFuncGetAttributes(&fa, kern));
+        staticSmem = fa.sharedSizeBytes;
         if (dev < 64) attrSet[dev] = true;
     }
     // at least one 16-byte unit, also when no window is used
     const size_t smem = sizeof(T) * (size_t)cap > 16 ? sizeof(T) * (size_t)cap : 16;
+    // Shared-memory carve-out: what MINB CTAs of this launch take (static +
+    // window + the 1 KB the system reserves per CTA), the rest stays L1,
+    // where the gathers outside the window and the matrix stream's loads in
+    // flight land.
+    {
+        const size_t smPerSm = dp.smem_per_sm ? dp.smem_per_sm : 233472;
+        const size_t need = (size_t)MINB * (staticSmem + smem + 1024);
+        int pct = (int)((need * 100 + smPerSm - 1) / smPerSm);
+        if (pct > 100) pct = 100;
+        MXS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+    }
     // Whole waves: CTAs hold equal nonzero counts, so the range length is
     // picked to make the CTA count a multiple of the CTAs resident at once.
     int perSm = 0;
@@ -225,7 +279,10 @@ spmv_status_t run_band(int block, int E, int tilesPerWarp, int winK, const int* 
     if (block == 512 && E == 16) MXS_WIN(512, 16, 2);
     else if (block == 512 && E == 8) MXS_WIN(512, 8, 2);
     else if (block == 1024 && E == 16) MXS_WIN(1024, 16, 1);
-    else if (block == 1024 && E == 8) MXS_WIN(1024, 8, wide ? 1 : 2);
+    else if (block == 1024 && E == 8 && !wide)  // one CTA per SM, the next tile's loads in flight
+        st = launch_window<T, 8, 1024, 1, true>(tileRow, tiles, carryRow, carryVal, errFlag, a, numCols, tilesPerWarp,
+                                                winK, tileBits, test, s);
+    else if (block == 1024 && E == 8) MXS_WIN(1024, 8, 1);
     else if (block == 256 && E == 16) MXS_WIN(256, 16, wide ? 3 : 4);
     else if (block == 256 && E == 8) MXS_WIN(256, 8, 4);
     else MXS_FAIL(SPMV_ERROR_INTERNAL, "unsupported band shape block=%d ept=%d", block, E);

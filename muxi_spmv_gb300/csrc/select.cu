@@ -46,8 +46,10 @@ static bool variant_applicable(const spmv_variant_t& v, int R, int N, long long 
 }
 
 // Predicted log-time gap under which the learned pick counts as uncertain
-// (SPMV_SELECT_LEARNED_FALLBACK): 0.05, about 5%.
-constexpr float kFallbackMargin = 0.05f;
+// (SPMV_SELECT_LEARNED_FALLBACK): 0.12, about 12%; at most kFallbackMax
+// candidates (the pick included) are timed unless topK says otherwise.
+constexpr float kFallbackMargin = 0.12f;
+constexpr int kFallbackMax = 4;
 
 static bool same_variant(const spmv_variant_t& a, const spmv_variant_t& b) {
     return a.kernel == b.kernel && a.blockSize == b.blockSize && a.threadsPerRow == b.threadsPerRow &&
@@ -127,8 +129,8 @@ spmv_status_t spmv_select(spmv_handle_t* h, spmv_select_mode_t mode, spmv_mlp_t 
             if (mode == SPMV_SELECT_LEARNED_TOPK && topK > 1) k = std::min<int>(topK, (int)order.size());
             if (mode == SPMV_SELECT_LEARNED_FALLBACK) {
                 // Low confidence: other variants predicted within kFallbackMargin
-                // of the best are timed too (at most topK, default 3).
-                const int kmax = std::min<int>(topK > 1 ? topK : 3, (int)order.size());
+                // of the best are timed too (at most topK, default kFallbackMax).
+                const int kmax = std::min<int>(topK > 1 ? topK : kFallbackMax, (int)order.size());
                 while (k < kmax && pred[order[k]] - pred[order[0]] <= kFallbackMargin) ++k;
             }
             if (k > 1) {

@@ -18,7 +18,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (NUM_FEATURES, SELECT_AUTOTUNE, SELECT_HEURISTIC, SELECT_LEARNED,  # noqa: F401
-                   SELECT_LEARNED_TOPK, SELECT_LEARNED_FALLBACK, FALLBACK_MARGIN, SPMV_TYPE_DOUBLE, SPMV_TYPE_FLOAT, GenParams, Variant, check, lib)
+                   SELECT_LEARNED_TOPK, SELECT_LEARNED_FALLBACK, FALLBACK_MARGIN, FALLBACK_MAX, SPMV_TYPE_DOUBLE, SPMV_TYPE_FLOAT, GenParams, Variant, check, lib)
 from .api import GenSpec, SpmvHandle, _ptr, _stream_ptr, _torch
 
 DEFAULT_MODEL = Path(__file__).resolve().parent / "data" / "selector_gb300.mxsmlp"
@@ -108,6 +108,8 @@ def variant_name(v: Variant) -> str:
         return f"csr5r_b{v.blockSize}_e{v.itemsPerThread}_r{per}{pf}"
     if v.kernel == 8:
         return f"stream_b{v.blockSize}_e{v.itemsPerThread}_s{v.threadsPerRow}"
+    if v.kernel == 7:  # window kernel: tiles per warp of a range, window in 1,024-element units
+        return f"band_b{v.blockSize}_e{v.itemsPerThread}_t{v.threadsPerRow}_w{v.vectorWidth}"
     if v.kernel in (3, 4, 7):
         return f"{name}_b{v.blockSize}_e{v.itemsPerThread}"
     return f"{name}_b{v.blockSize}"
@@ -231,11 +233,12 @@ def select(handle: SpmvHandle, A, mode: int = SELECT_LEARNED, model: MLP | None 
 
 def set_selector(handle: SpmvHandle, model: MLP | None, mode: int = SELECT_LEARNED):
     """Makes AUTO plans on `handle` use `model` (None clears it); mode
-    SELECT_LEARNED_FALLBACK also times the variants predicted within 5%."""
+    SELECT_LEARNED_FALLBACK also times the variants predicted within 12%
+    (at most 4 candidates)."""
     check(lib().spmv_set_selector(handle.raw, model.raw if model is not None else None), "spmv_set_selector")
     check(lib().spmv_set_selector_mode(handle.raw, mode), "spmv_set_selector_mode")
 
 
 __all__ = ["DeviceCSR", "gen_device", "gen_device_vector", "matrix_features", "variant_space", "variant_name",
            "autotune", "MLP", "select", "set_selector", "DEFAULT_MODEL", "SELECT_HEURISTIC", "SELECT_LEARNED",
-           "SELECT_AUTOTUNE", "SELECT_LEARNED_TOPK", "SELECT_LEARNED_FALLBACK", "FALLBACK_MARGIN", "NUM_FEATURES"]
+           "SELECT_AUTOTUNE", "SELECT_LEARNED_TOPK", "SELECT_LEARNED_FALLBACK", "FALLBACK_MARGIN", "FALLBACK_MAX", "NUM_FEATURES"]

@@ -151,8 +151,8 @@ def heuristic_variant(R: int, N: int) -> Variant:
     return Variant(api.KERNEL_VECTOR, 256, 32, 0, 1)
 
 
-def label_one(handle, seed: int, max_rows: int, max_nnz: int):
-    """Generates, featurises and autotunes one corpus matrix."""
+def corpus_matrix(seed: int, max_rows: int, max_nnz: int):
+    """The corpus matrix of `seed` on the device: (matrix, law, mean row length)."""
     import torch
     spec, law, m = spec_for_seed(seed, max_rows, max_nnz)
     if law == "powerlaw":  # no device law: host generator, copied over
@@ -164,6 +164,13 @@ def label_one(handle, seed: int, max_rows: int, max_nnz: int):
     else:
         A = selector.gen_device(spec)
     torch.cuda.synchronize()
+    return A, law, m
+
+
+def label_one(handle, seed: int, max_rows: int, max_nnz: int):
+    """Generates, featurises and autotunes one corpus matrix."""
+    import torch
+    A, law, m = corpus_matrix(seed, max_rows, max_nnz)
     feats = selector.matrix_features(A).cpu().numpy()
     space = selector.variant_space()
     cands = space + [heuristic_variant(A.numRows, A.nnz)]
@@ -202,6 +209,54 @@ def cmd_corpus(a):
         if a.time_limit and el > a.time_limit:
             print("time limit reached; rerun to resume", flush=True)
             break
+
+
+def cmd_relabel(a):
+    """Re-times one variant of the space (index a.index) on every record of
+    a corpus, regenerating each matrix from its seed (its rows, columns and
+    nonzeros must match the record), in resumable chunks under a.out; once
+    every chunk is there, writes the corpus with that column replaced to
+    a.merged."""
+    import torch
+    data = load_corpus(a.corpus)
+    meta = data["meta"]
+    space = selector.variant_space()
+    if not 0 <= a.index < len(space):
+        raise SystemExit(f"index {a.index} outside the variant space of {len(space)}")
+    v = space[a.index]
+    out = Path(a.out)
+    out.mkdir(parents=True, exist_ok=True)
+    handle = api.SpmvHandle()
+    torch.cuda.init()
+    t_start = time.perf_counter()
+    n = len(meta)
+    for c0 in range(0, n, a.chunk):
+        path = out / f"relabel_{a.index:02d}_{c0:06d}.npy"
+        if path.exists():
+            continue
+        col = []
+        for i in range(c0, min(c0 + a.chunk, n)):
+            A, _, _ = corpus_matrix(int(meta[i, 0]), a.max_rows, a.max_nnz)
+            if (A.numRows, A.numCols, A.nnz) != tuple(int(z) for z in meta[i, 2:5]):
+                raise SystemExit(f"seed {int(meta[i, 0])}: regenerated shape differs from the record")
+            ms, _ = selector.autotune(handle, A, [v], repeats=0)
+            col.append(float(ms[0]))
+            del A
+            torch.cuda.empty_cache()
+        tmp = out / f".relabel_{a.index:02d}_{c0:06d}.tmp.npy"
+        np.save(tmp, np.array(col, np.float32))
+        tmp.rename(path)
+        el = time.perf_counter() - t_start
+        print(f"chunk {c0}: {len(col)} matrices, {el:.0f}s elapsed", flush=True)
+        if a.time_limit and el > a.time_limit:
+            print("time limit reached; rerun to resume", flush=True)
+            return
+    parts = [np.load(out / f"relabel_{a.index:02d}_{c0:06d}.npy") for c0 in range(0, n, a.chunk)]
+    data = dict(data)
+    data["ms"] = data["ms"].copy()
+    data["ms"][:, a.index] = np.concatenate(parts)
+    save_corpus(data, a.merged)
+    print(f"wrote {a.merged}", flush=True)
 
 
 def load_corpus(spec: str) -> dict:
@@ -251,7 +306,7 @@ def learned_picks(pred: np.ndarray, ms_space: np.ndarray):
 
 
 def fallback_regrets(pred: np.ndarray, ms_space: np.ndarray, margin: float = selector.FALLBACK_MARGIN,
-                     kmax: int = 3):
+                     kmax: int = selector.FALLBACK_MAX):
     """SELECT_LEARNED_FALLBACK on recorded times: the learned pick plus the
     variants predicted within `margin` of it (at most kmax), fastest of them.
     Returns (regret per matrix, candidates timed per matrix)."""
@@ -403,6 +458,15 @@ def main(argv=None):
     c.add_argument("--max-rows", type=int, default=10_000_000)
     c.add_argument("--max-nnz", type=int, default=600_000_000)
     c.add_argument("--time-limit", type=float, default=0.0, help="seconds; stop after the chunk that passes it")
+    r = sub.add_parser("relabel")
+    r.add_argument("--corpus", required=True)
+    r.add_argument("--index", type=int, required=True, help="variant space index to re-time")
+    r.add_argument("--out", required=True, help="directory of resumable chunks")
+    r.add_argument("--merged", required=True, help="corpus .npz written once every chunk is done")
+    r.add_argument("--chunk", type=int, default=200)
+    r.add_argument("--max-rows", type=int, default=10_000_000)
+    r.add_argument("--max-nnz", type=int, default=600_000_000)
+    r.add_argument("--time-limit", type=float, default=0.0, help="seconds; stop after the chunk that passes it")
     t = sub.add_parser("train")
     t.add_argument("--corpus", required=True)
     t.add_argument("--model", required=True)
@@ -419,7 +483,7 @@ def main(argv=None):
     e.add_argument("--cost", action="store_true")
     e.add_argument("--report")
     a = p.parse_args(argv)
-    {"corpus": cmd_corpus, "train": cmd_train, "evaluate": cmd_evaluate}[a.cmd](a)
+    {"corpus": cmd_corpus, "relabel": cmd_relabel, "train": cmd_train, "evaluate": cmd_evaluate}[a.cmd](a)
 
 
 if __name__ == "__main__":

@@ -331,7 +331,8 @@ def test_select_modes(mx, sel, cuda, handle):
     assert ik in list(np.argsort(pred, kind="stable")[:3])
     # fallback: the pick, or one of the variants predicted within the margin
     vf, iff = sel.select(handle, A, sel.SELECT_LEARNED_FALLBACK, model)
-    near = [i for i in np.argsort(pred, kind="stable")[:3] if pred[i] - pred.min() <= sel.FALLBACK_MARGIN + 1e-6]
+    near = [i for i in np.argsort(pred, kind="stable")[:sel.FALLBACK_MAX]
+            if pred[i] - pred.min() <= sel.FALLBACK_MARGIN + 1e-6]
     assert iff in near and space[iff].as_dict() == vf.as_dict()
     with pytest.raises(mx.SpmvError):
         sel.select(handle, A, sel.SELECT_LEARNED, None)
@@ -360,7 +361,8 @@ def test_auto_plan_with_registered_selector(mx, sel, cuda):
     space = sel.variant_space()
     plan2 = mx.Plan(h, A)
     key = lambda v: (v.kernel, v.blockSize, v.threadsPerRow, v.itemsPerThread, v.vectorWidth)
-    near = [key(space[i]) for i in np.argsort(pred, kind="stable")[:3] if pred[i] - pred[il] <= sel.FALLBACK_MARGIN + 1e-6]
+    near = [key(space[i]) for i in np.argsort(pred, kind="stable")[:sel.FALLBACK_MAX]
+            if pred[i] - pred[il] <= sel.FALLBACK_MARGIN + 1e-6]
     assert key(plan2.variant) in near or key(plan2.variant) == key(vl)
     y2 = cuda.zeros(A.numRows, device="cuda")
     plan2.exec(cuda.from_numpy(x).cuda(), y2)

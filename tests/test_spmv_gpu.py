@@ -107,6 +107,7 @@ def test_variants_match_oracle(mx, cuda, cases, var, dtype):
 # 1K and 2K windows leave most gathers of the larger cases outside the window.
 PLAN_VARIANTS = [("band", 7, 512, 16, 0, 0), ("band", 7, 512, 8, 0, 0), ("band", 7, 1024, 16, 0, 2),
                  ("band", 7, 256, 8, 1, 1), ("band", 7, 256, 16, 2, 3), ("band", 7, 1024, 8, 4, 16),
+                 ("band", 7, 1024, 8, 16, 25), ("band", 7, 1024, 8, 0, 0),
                  ("csr5_512", 4, 256, 16, 4, 0), ("csr5_128", 4, 256, 4, 4, 0),
                  ("csr5o_128", 4, 256, 4, 32, 0), ("csr5o_256", 4, 256, 8, 32, 0), ("csr5o_512", 4, 256, 16, 32, 0),
                  ("csr5o_b128", 4, 128, 8, 32, 0), ("csr5o_b512", 4, 512, 8, 32, 0), ("csr5o_b1024", 4, 1024, 8, 32, 0),
