@@ -38,7 +38,7 @@ static const spmv_variant_t kSpace[] = {
     {SPMV_KERNEL_CSR5, 256, 0, 8, 32},
     {SPMV_KERNEL_CSR5, 128, 0, 16, 32},
     {SPMV_KERNEL_CSR5, 512, 0, 8, 32},
-    {SPMV_KERNEL_BAND, 1024, 25, 8, 16},
+    {SPMV_KERNEL_BAND, 1024, 25, 8, 14},
     {SPMV_KERNEL_ELL, 256, 0, 0, 1},
     // block ranges, one per resident block (contiguous tiles per SM)
     {SPMV_KERNEL_CSR5, 1024, SPMV_RANGE_PER_RESIDENT_BLOCK, 16, SPMV_CSR5_ORDERED},

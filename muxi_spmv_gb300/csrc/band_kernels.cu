@@ -118,7 +118,7 @@ __device__ __forceinline__ bool window_wait(unsigned long long* bar, long long l
 // tiles one at a time from a shared counter (neighbouring rows in flight
 // together, no block waits on one long tile).  Dynamic shared memory: the
 // window, winCap elements.
-template <typename T, int E, int BLOCK, int MINB, bool PF = false>
+template <typename T, int E, int BLOCK, int MINB, bool PF = false, bool VEC = false>
 __global__ void __launch_bounds__(BLOCK, MINB)
 csr5_window_kernel(int numRows, int numCols, int nnz, const int* __restrict__ rowPtr,
                    const int* __restrict__ colIdx, const T* __restrict__ values, const T* __restrict__ x,
@@ -159,7 +159,7 @@ csr5_window_kernel(int numRows, int numCols, int nnz, const int* __restrict__ ro
 
     int t = tb + w;
     OrderedLoad<T, E> L;
-    if (t < te) csr5_ordered_load<T, E>(L, t, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
+    if (t < te) csr5_ordered_load<T, E, VEC>(L, t, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
     // every thread waits (also warps without a tile: the CTA stays until the copy has landed)
     if (span > 0 && !window_wait(&bar, waitLimit, inject, errFlag)) return;
     int spanAfterWait = span;
@@ -172,9 +172,10 @@ csr5_window_kernel(int numRows, int numCols, int nnz, const int* __restrict__ ro
             if (lane == 0) next = atomicAdd(&sNext, 1);
             next = __shfl_sync(kFull, next, 0);
             if (next < te)
-                csr5_ordered_load<T, E>(nxt, next, lane, numRows, nnz, colIdx, values, tileRow, tiles, tileBits);
-            csr5_ordered_compute<T, E, true>(L, t, lane, nnz, rowPtr, gather, y, alpha, beta, bz, tiles, carryRow,
-                                             carryVal, noEmpty, sRpAll[w], sPAll[w], useBits, plain);
+                csr5_ordered_load<T, E, VEC>(nxt, next, lane, numRows, nnz, colIdx, values, tileRow, tiles,
+                                             tileBits);
+            csr5_ordered_compute<T, E, true, VEC>(L, t, lane, nnz, rowPtr, gather, y, alpha, beta, bz, tiles,
+                                                  carryRow, carryVal, noEmpty, sRpAll[w], sPAll[w], useBits, plain);
             L = nxt;
             t = next;
         }
@@ -209,11 +210,11 @@ static int default_window(const DeviceProps& dp) {
     return (int)(elems < 0 ? 0 : elems);
 }
 
-template <typename T, int E, int BLOCK, int MINB, bool PF = false>
+template <typename T, int E, int BLOCK, int MINB, bool PF = false, bool VEC = false>
 static spmv_status_t launch_window(const int* tileRow, long long tiles, int* carryRow, T* carryVal, int* errFlag,
                                    const RowsArgs<T>& a, int numCols, int tilesPerWarp, int winK,
                                    const unsigned* bits, const BandTest& test, cudaStream_t s) {
-    auto kern = csr5_window_kernel<T, E, BLOCK, MINB, PF>;
+    auto kern = csr5_window_kernel<T, E, BLOCK, MINB, PF, VEC>;
     int dev = 0;
     MXS_CUDA(cudaGetDevice(&dev));
     const DeviceProps& dp = device_props(dev);
@@ -279,10 +280,24 @@ spmv_status_t run_band(int block, int E, int tilesPerWarp, int winK, const int* 
     if (block == 512 && E == 16) MXS_WIN(512, 16, 2);
     else if (block == 512 && E == 8) MXS_WIN(512, 8, 2);
     else if (block == 1024 && E == 16) MXS_WIN(1024, 16, 1);
-    else if (block == 1024 && E == 8 && !wide)  // one CTA per SM, the next tile's loads in flight
-        st = launch_window<T, 8, 1024, 1, true>(tileRow, tiles, carryRow, carryVal, errFlag, a, numCols, tilesPerWarp,
-                                                winK, tileBits, test, s);
-    else if (block == 1024 && E == 8) MXS_WIN(1024, 8, 1);
+    else if (block == 1024 && E == 8) {
+        if constexpr (!wide) {
+            // one CTA per SM, the next tile's loads in flight; with 16-byte
+            // aligned colIdx / values each lane loads four consecutive
+            // nonzeros per instruction (a quarter of the load instructions
+            // and of the hand-off stores: this kernel is bound by issue)
+            const bool vec = (reinterpret_cast<uintptr_t>(a.colIdx) & 15) == 0 &&
+                             (reinterpret_cast<uintptr_t>(a.values) & 15) == 0;
+            if (vec)
+                st = launch_window<T, 8, 1024, 1, true, true>(tileRow, tiles, carryRow, carryVal, errFlag, a, numCols,
+                                                              tilesPerWarp, winK, tileBits, test, s);
+            else
+                st = launch_window<T, 8, 1024, 1, true>(tileRow, tiles, carryRow, carryVal, errFlag, a, numCols,
+                                                        tilesPerWarp, winK, tileBits, test, s);
+        } else {
+            MXS_WIN(1024, 8, 1);
+        }
+    }
     else if (block == 256 && E == 16) MXS_WIN(256, 16, wide ? 3 : 4);
     else if (block == 256 && E == 8) MXS_WIN(256, 8, 4);
     else MXS_FAIL(SPMV_ERROR_INTERNAL, "unsupported band shape block=%d ept=%d", block, E);

@@ -156,7 +156,17 @@ struct OrderedLoad {
     T v[E];
 };
 
-template <typename T, int E>
+// VEC (FP32, E a multiple of 4, 16-byte aligned colIdx and values): each
+// 128-nonzero chunk of the tile is loaded with one 16-byte load per lane,
+// lane l taking nonzeros 4l .. 4l+3 of the chunk, so element e of lane l is
+// nonzero 128 * (e / 4) + 4l + e % 4 of the tile (a quarter of the load
+// instructions).
+template <int E, bool VEC>
+__device__ __forceinline__ int ordered_pos(int lane, int e) {
+    return VEC ? 128 * (e >> 2) + 4 * lane + (e & 3) : lane + 32 * e;
+}
+
+template <typename T, int E, bool VEC = false>
 __device__ __forceinline__ void csr5_ordered_load(OrderedLoad<T, E>& L, long long t, int lane, int numRows, int nnz,
                                                   const int* __restrict__ colIdx, const T* __restrict__ values,
                                                   const int* __restrict__ tileRow, long long tiles,
@@ -164,6 +174,35 @@ __device__ __forceinline__ void csr5_ordered_load(OrderedLoad<T, E>& L, long lon
     constexpr int SIGMA = 32 * E;
     const int tStart = (int)t * SIGMA;
     L.bits = tileBits ? __ldg(tileBits + t * E + (lane % E)) : 0u;
+    if constexpr (VEC) {
+        static_assert(sizeof(T) == 4 && E % 4 == 0, "16-byte tile loads: FP32, E a multiple of 4");
+        if (tStart + SIGMA <= nnz) {
+#pragma unroll
+            for (int k = 0; k < E / 4; ++k) {
+                const int o = tStart + 128 * k + 4 * lane;
+                const int4 c4 = ld_stream4(colIdx + o);
+                const float4 v4 = ld_stream4(reinterpret_cast<const float*>(values) + o);
+                L.c[4 * k] = c4.x;
+                L.c[4 * k + 1] = c4.y;
+                L.c[4 * k + 2] = c4.z;
+                L.c[4 * k + 3] = c4.w;
+                L.v[4 * k] = v4.x;
+                L.v[4 * k + 1] = v4.y;
+                L.v[4 * k + 2] = v4.z;
+                L.v[4 * k + 3] = v4.w;
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const int j = tStart + ordered_pos<E, true>(lane, e);
+                L.c[e] = j < nnz ? ld_stream(colIdx + j) : 0;
+                L.v[e] = j < nnz ? ld_stream(values + j) : T(0);
+            }
+        }
+        L.rFirst = __ldg(tileRow + t);
+        L.rLast = t + 1 < tiles ? __ldg(tileRow + t + 1) : numRows - 1;
+        return;
+    }
     if (tStart + SIGMA <= nnz) {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
@@ -189,7 +228,7 @@ __device__ __forceinline__ void csr5_ordered_load(OrderedLoad<T, E>& L, long lon
 // then the gathered x, go through the same region and each term is one FMA
 // -- on GB300 the FP64 pipe, not memory, bounds an FP64 SpMV, and a product
 // plus an add cost it two instructions per nonzero where the FMA costs one.
-template <typename T, int E, typename Rows>
+template <typename T, int E, bool VEC, typename Rows>
 __device__ __forceinline__ void ordered_handoff(const T (&v)[E], const T (&g)[E], int lane, T* sP, Rows rows) {
     if constexpr (sizeof(T) == 8) {
         T a[E];
@@ -204,10 +243,21 @@ __device__ __forceinline__ void ordered_handoff(const T (&v)[E], const T (&g)[E]
         __syncwarp();
         rows([&](T r, int e) { return fma(a[e], sP[ordered_slot<T, E>(lane * E + e)], r); }, nullptr);
     } else {
+        if constexpr (VEC) {
+            // lane l's elements 4k .. 4k+3 are nonzeros 4(32k + l) .. +3: one
+            // 16-byte word, 32 consecutive words per store (conflict-free
+            // under the swizzle: eight words of an aligned group per phase)
+            float4* w4 = reinterpret_cast<float4*>(sP);
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const int j = lane + 32 * e;
-            sP[swizzled_word(j >> 2) * 4 + (j & 3)] = v[e] * g[e];
+            for (int k = 0; k < E / 4; ++k)
+                w4[swizzled_word(32 * k + lane)] = make_float4(v[4 * k] * g[4 * k], v[4 * k + 1] * g[4 * k + 1],
+                                                               v[4 * k + 2] * g[4 * k + 2], v[4 * k + 3] * g[4 * k + 3]);
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const int j = lane + 32 * e;
+                sP[swizzled_word(j >> 2) * 4 + (j & 3)] = v[e] * g[e];
+            }
         }
         __syncwarp();
         T p[E];
@@ -238,7 +288,7 @@ struct GlobalGather {
 
 // REUSE: the warp runs further tiles on the same shared regions afterwards.
 // gather(c): x[c].
-template <typename T, int E, bool REUSE, typename Gather>
+template <typename T, int E, bool REUSE, bool VEC = false, typename Gather>
 __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L, long long t, int lane, int nnz,
                                                      const int* __restrict__ rowPtr, Gather gather,
                                                      T* __restrict__ y, T alpha, T beta, bool bz, long long tiles,
@@ -264,7 +314,7 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
     }
 
     if (useBits) {
-        ordered_handoff<T, E>(L.v, g, lane, sP, [&](auto acc, T* sY) {
+        ordered_handoff<T, E, VEC>(L.v, g, lane, sP, [&](auto acc, T* sY) {
             csr5_tile_rows_bits<T, E>(acc, L.bits, rFirst, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal,
                                       plain, sY);
         });
@@ -280,7 +330,7 @@ __device__ __forceinline__ void csr5_ordered_compute(const OrderedLoad<T, E>& L,
             if (i < nRp) sRp[i] = __ldg(rowPtr + rFirst + i);
         }
     }
-    ordered_handoff<T, E>(L.v, g, lane, sP, [&](auto acc, T*) {
+    ordered_handoff<T, E, VEC>(L.v, g, lane, sP, [&](auto acc, T*) {
         csr5_tile_rows<T, E>(acc, rFirst, rLast, t, lane, nnz, y, alpha, beta, bz, carryRow, carryVal,
                              [&](int r) { return (staged && r >= rFirst) ? sRp[r - rFirst] : __ldg(rowPtr + r); },
                              noEmpty, plain);

@@ -68,7 +68,7 @@ def _variants(mx):
             mx.make_variant(mx.KERNEL_CSR5, 256, 0, 8, 1), mx.make_variant(mx.KERNEL_CSR5, 128, 0, 16, 32),
             mx.make_variant(mx.KERNEL_CSR5, 1024, R, 16, 32), mx.make_variant(mx.KERNEL_CSR5, 1024, R, 8, 64),
             mx.make_variant(mx.KERNEL_CSR5, 512, 3, 16, 64), mx.make_variant(mx.KERNEL_BAND, 512, 0, 16),
-            mx.make_variant(mx.KERNEL_BAND, 1024, 25, 8, 16), mx.make_variant(mx.KERNEL_BAND, 1024, 2, 8, 1),
+            mx.make_variant(mx.KERNEL_BAND, 1024, 25, 8, 14), mx.make_variant(mx.KERNEL_BAND, 1024, 2, 8, 1),
             mx.make_variant(mx.KERNEL_STREAM, 512), mx.make_variant(mx.KERNEL_ELL)]
 
 
