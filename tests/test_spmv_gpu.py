@@ -168,27 +168,29 @@ def test_band_unaligned_x_reads_global(mx, cuda, handle, cases, dtype):
     p.destroy()
 
 
-@pytest.mark.parametrize("kind", ["band", "stream"])
+@pytest.mark.parametrize("kind", ["band", "band1024", "stream"])
 def test_bulk_copy_wait_runs_out_and_reports(mx, cuda, handle, cases, kind):
     """Waits on bulk copies are bounded.  With one arrival of each copy
     barrier held back, the waits run out after 100,000 clocks; the kernel
     makes the arrivals itself so its copies land, returns, and the plan
     reports code 2 (BAND window) or 3 (STREAM tile slots) as SpmvError.  The
     context stays usable: the next normal execution of the same plan matches
-    the oracle."""
+    the oracle.  band1024 is the window kernel's shape the selector offers
+    (one 1,024-thread CTA per SM, next tile prefetched, 16-byte tile loads)."""
     torch = cuda
     rp, ci, v, cols = cases["powerlaw60k"]
     A = device_csr(mx, rp, ci, v, cols)
     xh = mx.gen_vector(cols, 77)
     x = torch.from_numpy(xh).cuda()
-    var = (mx.make_variant(mx.KERNEL_BAND, 512, 0, 16, 0) if kind == "band" else
-           mx.make_variant(mx.KERNEL_STREAM, 512, 3, 16, 0))
+    var = {"band": mx.make_variant(mx.KERNEL_BAND, 512, 0, 16, 0),
+           "band1024": mx.make_variant(mx.KERNEL_BAND, 1024, 25, 8, 14),
+           "stream": mx.make_variant(mx.KERNEL_STREAM, 512, 3, 16, 0)}[kind]
     p = mx.Plan(handle, A, var)
     y = torch.zeros(A.numRows, device="cuda")
     p.inject_wait_timeout(True)
     p.exec(x, y)
     torch.cuda.synchronize()
-    with pytest.raises(mx.SpmvError, match="code 2" if kind == "band" else "code 3"):
+    with pytest.raises(mx.SpmvError, match="code 3" if kind == "stream" else "code 2"):
         p.device_error()
     assert p.device_error() == 0  # reading the word cleared it
     p.inject_wait_timeout(False)
@@ -197,7 +199,7 @@ def test_bulk_copy_wait_runs_out_and_reports(mx, cuda, handle, cases, kind):
     assert p.device_error() == 0
     check(y, np.zeros(A.numRows, np.float32), A, xh, 1.0, 0.0)
     p.destroy()
-    q = mx.Plan(handle, A)  # the default kernel has no bounded wait to inject into
+    q = mx.Plan(handle, A, mx.make_variant(mx.KERNEL_CSR5, 128, 0, 16, 32))  # no bounded wait to inject into
     with pytest.raises(mx.SpmvError):
         q.inject_wait_timeout(True)
     q.destroy()
