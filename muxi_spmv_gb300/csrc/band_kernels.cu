@@ -54,9 +54,9 @@ namespace mxs {
 // costs a few bank wavefronts where a global one costs about one L1 tag
 // lookup per lane, and only the lanes outside the window reach the L1.
 // Without one (span = 0: x not 16-byte aligned) it is the plain read-only
-// load.  The test on span is also measured to matter for speed: with it the
-// compiler keeps each gather apart from the surrounding work (4,550 against
-// 4,450 GB/s on the 8M-row power law without it).  What keeps the shared
+// load.  The test on span also changes how the compiled code schedules the
+// gathers, and measured faster than the same loads without it (4,550 against
+// 4,450 GB/s on the 8M-row power law).  What keeps the shared
 // loads after the wait for the window's bulk copy is their input `span`,
 // which passes through a volatile move placed after that wait.
 template <typename T>
@@ -195,11 +195,12 @@ bool band_shape_supported(int block, int E) {
     return (block == 256 || block == 512 || block == 1024) && (E == 8 || E == 16);
 }
 
-// Default window capacity (elements) of a shape: the largest multiple of
-// 1,024 elements that keeps MINB CTAs per SM within the SM's shared memory
-// (228 KB, 1 KB of it reserved per CTA), capped at 40,960.
+// Largest window (elements) of a shape: the largest multiple of 1,024
+// elements that keeps MINB CTAs per SM within the SM's shared memory (228 KB,
+// 1 KB of it reserved per CTA), capped at 40,960.  Windows default to 16,384
+// elements (or this, if smaller): larger ones take L1 from the far gathers.
 template <typename T, int E, int BLOCK, int MINB>
-static int default_window(const DeviceProps& dp) {
+static int max_window(const DeviceProps& dp) {
     constexpr size_t staticBytes = (BLOCK / 32) * (kOrderedRpCap * sizeof(int) + ordered_slots<T, E>() * sizeof(T)) + 64;
     const size_t smPerSm = dp.smem_per_sm ? dp.smem_per_sm : 233472;
     const size_t perCta = smPerSm / MINB - 1024;
@@ -218,7 +219,7 @@ static spmv_status_t launch_window(const int* tileRow, long long tiles, int* car
     int dev = 0;
     MXS_CUDA(cudaGetDevice(&dev));
     const DeviceProps& dp = device_props(dev);
-    const int maxWin = default_window<T, E, BLOCK, MINB>(dp);
+    const int maxWin = max_window<T, E, BLOCK, MINB>(dp);
     int cap = winK > 0 ? winK * 1024 : 16384;
     if (cap > maxWin) cap = maxWin;
     const bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0;
