@@ -265,7 +265,10 @@ typedef enum {
                                   gathers that fall in a bulk-copied shared-memory
                                   window of x around its rows from there (FP32 at
                                   1024 threads and 8 per lane: one CTA per SM, the
-                                  next tile's loads in flight)                      */
+                                  next tile's loads in flight, 16-byte tile loads
+                                  when colIdx and values are 16-byte aligned).  The
+                                  launch sets the kernel's shared-memory carve-out
+                                  preference to what its CTAs use              */
     SPMV_KERNEL_STREAM = 8     /* ordered CSR5 tiles of 32*itemsPerThread nonzeros, one
                                   CTA per SM over a contiguous tile range; each warp's
                                   next tiles are bulk-copied (TMA) into a ring of
