@@ -308,6 +308,52 @@ def test_plans(mx, cuda, handle, cases):
     p.destroy()
 
 
+def test_f64_auto_takes_block_ranges_on_large_near_diagonal_matrices(mx, cuda, handle, cases):
+    """FP64 AUTO plans (no model) take one range of tiles per resident block
+    when every warp of those ranges gets at least 8 tiles and most sampled
+    nonzeros lie within 4,096 columns of the diagonal; otherwise the FP64
+    default (one 256-nonzero tile per warp, 128-thread blocks).  The ranges'
+    result matches the oracle at the FP64 bound."""
+    torch = cuda
+    from muxi_spmv_gb300 import workloads as W
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    need = sms * 32 * 8 * 256  # nonzeros that give every warp 8 tiles of 256
+    R = mx.RANGE_PER_RESIDENT_BLOCK
+
+    def auto_variant(rp, ci, v, cols):
+        A = device_csr(mx, rp, ci, v.astype(np.float64), cols)
+        p = mx.Plan(handle, A)
+        pv = p.variant
+        return A, p, (pv.kernel, pv.blockSize, pv.threadsPerRow, pv.itemsPerThread, pv.vectorWidth)
+
+    # near-diagonal and large: a 2D 5-point grid of about need/5 * 1.2 rows
+    spec = W.scaled("stencil2d_4096", int(need / 5 * 1.2), seed=7)
+    rp, ci, v = mx.generate(spec)
+    assert rp[-1] >= need
+    A, p, key = auto_variant(rp, ci, v, spec.numCols)
+    assert key == (mx.KERNEL_CSR5, 1024, R, 8, 32)
+    xh = mx.gen_vector(spec.numCols, 5, dtype=np.float64)
+    y = torch.zeros(A.numRows, dtype=torch.float64, device="cuda")
+    p.exec(torch.from_numpy(xh).cuda(), y)
+    torch.cuda.synchronize()
+    check(y, np.zeros(A.numRows), A, xh, 1.0, 0.0)
+    p.destroy()
+    del A
+    # large but uniform columns: the default
+    spec = W.scaled("poisson16k", int(need / 12 * 1.2), seed=8)
+    rp, ci, v = mx.generate(spec)
+    assert rp[-1] >= need
+    A, p, key = auto_variant(rp, ci, v, spec.numCols)
+    assert key == (mx.KERNEL_CSR5, 128, 0, 8, 32)
+    p.destroy()
+    del A
+    # small: the default
+    rp, ci, v, cols = cases["powerlaw60k"]
+    A, p, key = auto_variant(rp, ci, v, cols)
+    assert key == (mx.KERNEL_CSR5, 128, 0, 8, 32)
+    p.destroy()
+
+
 def test_f64_interior_tiles_over_wide_exponent_ranges(mx, cuda, handle):
     """FP64 tiles inside one row sum their lanes in 64-bit fixed point below
     the largest lane's exponent: long rows whose products span 1e-300 to
