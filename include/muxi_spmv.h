@@ -771,7 +771,9 @@ SPMV_API spmv_status_t spmv_select(spmv_handle_t* handle, spmv_select_mode_t mod
                                    const int* colIdx, const void* values, spmv_variant_t* out, int* spaceIndex);
 /* Registers (model != NULL) or clears a selector model on the handle: FP32
  * plans created with SPMV_KERNEL_AUTO then take the learned pick (the model
- * is trained on FP32 timings; FP64 AUTO plans keep the FP64 default).  The
+ * is trained on FP32 timings; FP64 AUTO plans keep their own rule: one
+ * range of tiles per SM on large matrices whose nonzeros mostly lie within
+ * 4,096 columns of the diagonal, else 256-nonzero tiles per warp).  The
  * handle borrows the model; it must outlive the handle's use of it. */
 SPMV_API spmv_status_t spmv_set_selector(spmv_handle_t* handle, spmv_mlp_t model);
 /* How AUTO plans on this handle use the registered model:
